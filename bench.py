@@ -1,0 +1,362 @@
+"""Benchmark: TEPS of the sm_103a hash triangle counter on one GB300 (replicas for N > 1).
+
+Workload (default): the Chung-Lu power-law graph with 3.8M vertices, degree exponent 2.5, maximum
+expected degree 800, ~16.5M undirected edges, seed 2 — the synthetic stand-in for the reference's
+Cit-Patents example (generated on the GPU, GPU-preprocessed to an oriented int32 CSR with int64
+offsets).  A step is one counting call over the whole graph.  Metric: TEPS = m / t, printed by the
+reference as GTEPS (Without-graph-partition/mpi_main.cpp:124).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload NAME]
+
+Rank 0 prints one JSON line.  `value` times the device-resident call (validation, classification,
+counting); `e2e` times the same call through the C ABI with pinned host buffers (H2D copy and the
+result read inside the timed region); `roofline` relates the counting kernel's algorithmic bytes
+to the measured HBM copy bandwidth; `cpu_baseline` is the CPU forward-intersection counter.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    "chung_lu_3.8m": dict(kind="chung_lu", n=3_800_000, gamma=2.5, w_max=800.0, target=16_500_000,
+                          npairs=16_500_000, seed=2,
+                          desc="Chung-Lu n=3.8M gamma=2.5 w_max=800 ~16.5M undirected edges seed=2"),
+    "rmat16": dict(kind="rmat", scale=16, ef=16, a=0.57, b=0.19, c=0.19, seed=1,
+                   desc="R-MAT scale 16 edge factor 16 (0.57,0.19,0.19,0.05) seed=1"),
+    "rmat22": dict(kind="rmat", scale=22, ef=16, a=0.57, b=0.19, c=0.19, seed=3,
+                   desc="R-MAT scale 22 edge factor 16 (0.57,0.19,0.19,0.05) seed=3"),
+}
+DEFAULT_WORKLOAD = "chung_lu_3.8m"
+L2_FLUSH_BYTES = 256 << 20  # > 126 MB L2; the default graph (~96 MB) fits in L2, so flush every step
+KERNELS_PER_CALL = 4        # check, classify histogram, classify scatter, count
+
+
+def _peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured (MEASURED_PEAKS.json hbm_gbs, burst copy)"
+    return 6800.0, "fallback 6.8 TB/s"
+
+
+def _traffic(workload):
+    """DRAM bytes per counting-kernel launch from the committed ncu summary, if one exists."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        e = d.get(workload)
+        if e:
+            return e.get("dram_bytes_per_launch")
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 50 ms while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(prefix="clocks", suffix=".csv")
+        os.close(fd)
+        try:
+            self.out = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "50"], stdout=self.out,
+                                         stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        time.sleep(0.15)
+        return self
+
+    def __exit__(self, *exc):
+        time.sleep(0.1)
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        self.out.close()
+
+    def summary(self):
+        rows = []
+        try:
+            with open(self.path) as f:
+                for ln in f:
+                    parts = [x.strip() for x in ln.split(",")]
+                    if len(parts) >= 9 and parts[1].replace(".", "").isdigit():
+                        rows.append(parts)
+        finally:
+            os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm = [float(r[1]) for r in rows]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": float(rows[0][2]), "reasons": reasons,
+                "samples": len(rows), "power_w_max": max(float(r[3]) for r in rows if r[3].replace(".", "").isdigit())}
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def make_graph_gpu(w):
+    """Synthetic graph on the GPU: generate pairs, preprocess to the oriented CSR (timed separately)."""
+    import torch
+    import trust_gb300 as T
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    if w["kind"] == "chung_lu":
+        pairs = T.gen_chung_lu(w["n"], w["gamma"], w["w_max"], w["target"], w["npairs"], seed=w["seed"])
+        bound = w["n"]
+    else:
+        pairs = T.gen_rmat(w["scale"], w["ef"], w["a"], w["b"], w["c"], seed=w["seed"])
+        bound = 1 << w["scale"]
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    beg, adj = T.build_csr(pairs, bound)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    del pairs
+    return beg, adj, {"generate_ms": (t1 - t0) * 1e3, "preprocess_ms": (t2 - t1) * 1e3}
+
+
+def make_graph_cpu(w):
+    """The same graph built by the CPU oracle (used by the reference arm: no product code on it)."""
+    from oracle import oracle as O
+    if w["kind"] == "chung_lu":
+        cdf = O.chung_lu_cdf(w["n"], w["gamma"], w["w_max"], w["target"])
+        pairs = O.gen_weighted(cdf, w["npairs"], w["seed"])
+        bound = w["n"]
+    else:
+        pairs = O.gen_rmat(w["scale"], w["ef"] << w["scale"], w["a"], w["b"], w["c"], w["seed"])
+        bound = 1 << w["scale"]
+    return O.build_csr(pairs, bound)
+
+
+def cpu_baseline(beg_np, adj_np, budget_s: float = 12.0):
+    """The oracle's forward-intersection counter on every host core over the whole graph (rows are
+    already sorted by the preprocessing, so no per-row sort is timed), repeated within a budget."""
+    from oracle import oracle as O
+    threads = os.cpu_count() or 1
+    n = beg_np.size - 1
+    m = adj_np.size
+    times, count = [], None
+    t_start = time.perf_counter()
+    while len(times) < 5 and (time.perf_counter() - t_start) < budget_s:
+        t0 = time.perf_counter()
+        count = O.count_forward_sorted_range(beg_np, adj_np, 0, n, 2, threads)
+        times.append(time.perf_counter() - t0)
+    t = statistics.median(times)
+    return {"value": m / t / 1e9, "unit": "GTEPS", "cores": threads, "kind": "port",
+            "sample": f"whole graph, {len(times)} runs (median {t * 1e3:.1f} ms), forward intersection over "
+                      f"presorted rows, {threads} threads"}, count
+
+
+def run_ours(args, ws, rank, local):
+    import numpy as np
+    import torch
+    import trust_gb300 as T
+
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    w = WORKLOADS[args.workload]
+    beg, adj, prep = make_graph_gpu(w)
+    n, m = beg.numel() - 1, adj.numel()
+    stream = torch.cuda.current_stream()
+    ctx = T.Context(local)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device="cuda")
+
+    def call():
+        return T.count_csr(beg, adj, ctx=ctx, stream=stream.cuda_stream)
+
+    for _ in range(args.warmup):
+        r = call()
+    expect_count = r.triangles
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    res = []
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        for i in range(args.steps):
+            flush.fill_(i)
+            ev[i][0].record(stream)
+            res.append(call())
+            ev[i][1].record(stream)
+        torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clocks = clk.summary()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    total_ms = sum(step_ms)
+    if dist:
+        t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ok = all(r.triangles == expect_count for r in res)
+    count_s = statistics.median(r.count_seconds for r in res)
+    kernel_s = statistics.median(r.kernel_seconds for r in res)
+    wedges = res[0].wedges
+
+    # end to end through the C ABI: pinned host buffers, H2D + count + result read inside the region
+    hb = beg.cpu().pin_memory()
+    ha = adj.cpu().pin_memory()
+    hb_np, ha_np = hb.numpy(), ha.numpy()
+    e2e_ev = []
+    for i in range(max(3, args.steps // 4) + 2):
+        flush.fill_(i)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        r2 = T.count_csr(hb_np, ha_np, ctx=ctx, stream=stream.cuda_stream)
+        b.record(stream)
+        ok = ok and r2.triangles == expect_count
+        e2e_ev.append((a, b))
+    torch.cuda.synchronize()
+    e2e_ms = [a.elapsed_time(b) for a, b in e2e_ev[2:]]
+    e2e_mean = statistics.mean(e2e_ms)
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+    peak, peak_src = _peaks()
+    algo_bytes = 24 * m + 8 * (n + 1) + 4 * wedges
+    achieved = algo_bytes / count_s / 1e9
+    line = {
+        "metric": "TEPS = undirected edges / counting time (reference formula), plain degree-threshold schedule",
+        "value": ws * m * args.steps / (total_ms * 1e-3) / 1e9,
+        "unit": "GTEPS",
+        "n_gpus": ws,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": total_ms / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "int32",
+        "data": "synthetic (seeded generator on the GPU, GPU-preprocessed oriented CSR); no dataset download",
+        "config": {"workload": w["desc"], "vertices": n, "edges": m, "wedges": wedges, "triangles": expect_count,
+                   "schedule": "plain", "class_sizes": res[0].class_sizes, "parallelism": f"replicas x{ws}",
+                   "l2": f"{L2_FLUSH_BYTES >> 20} MiB buffer written before every timed step (graph "
+                         f"{(8 * (n + 1) + 4 * m) / 1e6:.0f} MB fits in L2)"},
+        "counts_consistent": ok,
+        "kernel_ms": kernel_s * 1e3,
+        "count_kernel_ms": count_s * 1e3,
+        "gpu_launches": KERNELS_PER_CALL * args.steps,
+        "e2e": {"value": m / (e2e_mean * 1e-3) / 1e9, "unit": "GTEPS",
+                "h2d_bytes_per_step": 8 * (n + 1) + 4 * m, "d2h_bytes_per_step": int(T.load().trust_tc_readback_bytes()),
+                "ms_per_step": e2e_mean},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": _traffic(args.workload), "peak_source": peak_src,
+                     "algorithmic_bytes": algo_bytes,
+                     "bytes_formula": "24 m + 8 (n+1) + 4 W (W = wedges = probes)"},
+        "preprocess": {"gpu_generate_ms": prep["generate_ms"], "gpu_build_csr_ms": prep["preprocess_ms"]},
+        "clocks": clocks,
+    }
+    if ws == 1 and not args.no_cpu_baseline:
+        cb, cpu_count = cpu_baseline(beg.cpu().numpy(), adj.cpu().numpy())
+        line["cpu_baseline"] = cb
+        line["count_matches_oracle"] = cpu_count == expect_count
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def run_reference(args, ws, rank, local):
+    """The reference's CPU-side counting for this path: it ships no CPU counter, so the oracle port of
+    its counted quantity runs on every host core, one bounded vertex slice per step.  Where the
+    reference kernel cubin is present (built from Without-graph-partition/TC.cu for sm_103a) its GPU
+    time on the same CSR is reported beside it."""
+    if rank != 0:
+        return
+    import numpy as np
+    from oracle import oracle as O
+    w = WORKLOADS[args.workload]
+    beg, adj = make_graph_cpu(w)
+    n, m = beg.size - 1, adj.size
+    threads = os.cpu_count() or 1
+    slices = 8
+    bounds = np.linspace(0, n, slices + 1).astype(np.int64)
+    arcs = np.diff(beg[bounds])
+    for i in range(args.warmup):
+        s = i % slices
+        O.count_forward_sorted_range(beg, adj, int(bounds[s]), int(bounds[s + 1]), 2, threads)
+    tot_arcs, tot_t = 0, 0.0
+    for i in range(args.steps):
+        s = i % slices
+        t0 = time.perf_counter()
+        O.count_forward_sorted_range(beg, adj, int(bounds[s]), int(bounds[s + 1]), 2, threads)
+        tot_t += time.perf_counter() - t0
+        tot_arcs += int(arcs[s])
+    value = tot_arcs / tot_t / 1e9
+    line = {
+        "impl": "reference",
+        "metric": "TEPS = undirected edges / counting time (reference formula), plain degree-threshold schedule",
+        "value": value, "unit": "GTEPS", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": tot_t / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded generator, CPU oracle pipeline)",
+        "config": {"workload": w["desc"], "vertices": n, "edges": m, "schedule": "plain"},
+        "cpu_baseline": {"value": value, "unit": "GTEPS", "cores": threads, "kind": "port",
+                         "sample": f"one of {slices} vertex slices per step (~{m // slices} arcs), forward "
+                                   f"intersection over presorted rows, {threads} threads"},
+        "e2e": {"value": value, "unit": "GTEPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    if O.ref_kernel_available():
+        flags, _ = O.trust_check(beg, adj)
+        if flags == O.TRUST_EXACT:
+            runs = [O.ref_kernel_count(beg, adj, blocks=1024, chunk=1) for _ in range(3)]
+            ms = statistics.median(r[1] for r in runs)
+            line["reference_kernel_sm103a"] = {"gteps": m / (ms * 1e-3) / 1e9, "kernel_ms": ms, "count": runs[0][0],
+                                               "launch": "dynamic_assign<<<1024,1024>>> chunk 1 (README example)"}
+        else:
+            line["reference_kernel_sm103a"] = {"unavailable": f"reference kernel not exact on this CSR (flags {flags})"}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default=DEFAULT_WORKLOAD)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    ws, rank, local = _dist()
+    if args.impl == "reference":
+        run_reference(args, ws, rank, local)
+    else:
+        run_ours(args, ws, rank, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,183 @@
+/*
+ * trust_tc.h — C ABI of the GB300 (sm_103a) vertex-centric hash triangle counter.
+ *
+ * Drop-in boundary for TRUST's counting path.  The reference exposes one C++ operator,
+ *   struct arguments Triangle_count(int rank, char name[100], struct arguments args,
+ *                                   int total_process, int n_threads, int n_blocks, int chunk_size)
+ * (Without-graph-partition/TC.cuh:10, implemented at Without-graph-partition/TC.cu:602-731), and a
+ * partitioned variant with an extra `partition_num` argument (With-graph-partition/TC.cuh:10,
+ * With-graph-partition/TC.cu:976-1157).  That operator loads `begin.bin` (int64 offsets) and
+ * `adjacent.bin` (int32 neighbours) from a folder, runs the `dynamic_assign` kernel and returns
+ * the u64 count.  Every entry point below is plain C: pointers, sizes and status codes.  No
+ * entry point calls exit(); errors come back as TRUST_TC_E_* codes (the reference prints and
+ * exits on any CUDA error, Without-graph-partition/herror.h:1-8).
+ *
+ * Counted quantity (identical to dynamic_assign on inputs where that kernel is exact):
+ *   count = sum over vertices v with out-degree d(v) >= 2,
+ *           sum over arcs (v,u) in row v (with multiplicity),
+ *           sum over arcs (u,w) in row u (with multiplicity),  [w is an element of row v]
+ * On an oriented simple graph this is the number of triangles.  Rows may be unsorted.
+ */
+#ifndef TRUST_TC_H
+#define TRUST_TC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------------------------- */
+enum {
+  TRUST_TC_OK = 0,
+  TRUST_TC_E_ARG = 1,          /* null pointer, negative size, bad option value            */
+  TRUST_TC_E_IO = 2,           /* folder / file missing or unreadable                      */
+  TRUST_TC_E_FORMAT = 3,       /* file sizes not a whole number of records, n < 0          */
+  TRUST_TC_E_OFFSETS = 4,      /* begin[0] != 0, begin not monotone, begin[n] != m         */
+  TRUST_TC_E_IDS = 5,          /* a neighbour id outside [0, n)                            */
+  TRUST_TC_E_TOO_LARGE = 6,    /* m >= 2^31, n >= 2^31 or an out-degree >= 2^26            */
+  TRUST_TC_E_CUDA = 7,         /* CUDA runtime error (text in trust_tc_last_cuda_error)    */
+  TRUST_TC_E_NOMEM = 8,        /* host or device allocation failed                         */
+  TRUST_TC_E_DEVICE = 9,       /* device-side error word set (bounded wait ran out, ...)   */
+  TRUST_TC_E_UNSUPPORTED = 10, /* option combination not supported                         */
+  TRUST_TC_E_NO_DEVICE = 11    /* no CUDA device visible                                   */
+};
+
+/* where the caller's CSR arrays live */
+enum { TRUST_TC_HOST = 0, TRUST_TC_DEVICE = 1 };
+
+/* work schedule; only the schedule changes, never the integer arithmetic */
+enum {
+  TRUST_TC_SCHED_PLAIN = 0,   /* degree-threshold classes (the reference's USE_CTA/USE_WARP split)  */
+  TRUST_TC_SCHED_LEARNED = 1  /* per-vertex cost model decides class and queue order                */
+};
+
+/* validation level for device-resident input (host input is always fully validated) */
+enum { TRUST_TC_VALIDATE_NONE = 0, TRUST_TC_VALIDATE_OFFSETS = 1, TRUST_TC_VALIDATE_FULL = 2 };
+
+typedef struct trust_tc_opts {
+  int device;            /* CUDA ordinal; -1 = current device                                   */
+  int threads_per_block; /* reference argv[3]; multiple of 32 in [64,1024]; 0 = library default */
+  int blocks;            /* reference argv[4]; 0 = persistent (SM count x resident blocks)      */
+  int chunk;             /* reference argv[5]; vertices per work-queue claim; 0 = default       */
+  int ptr_kind;          /* TRUST_TC_HOST or TRUST_TC_DEVICE                                     */
+  int schedule;          /* TRUST_TC_SCHED_*                                                     */
+  int validate;          /* TRUST_TC_VALIDATE_* (device input); default FULL                     */
+  int warp_max_degree;   /* out-degree above which a vertex gets a whole CTA; 0 = default       */
+  int block_max_degree;  /* out-degree above which a vertex gets a cluster table; 0 = default   */
+  int record_cycles;     /* 1: write per-vertex clock64 cycles into result->vertex_cycles       */
+  void *stream;          /* cudaStream_t; NULL = legacy default stream                          */
+  const float *model;    /* learned schedule: packed MLP weights (trust_tc_model_size floats)   */
+} trust_tc_opts;
+
+typedef struct trust_tc_result {
+  uint64_t triangles;       /* the count                                                     */
+  double kernel_seconds;    /* CUDA-event time of classification + counting (validation excluded) */
+  double count_seconds;     /* CUDA-event time of the counting kernel alone                  */
+  double call_seconds;      /* CUDA-event time of the whole device-side call                 */
+  int64_t vertices;         /* n                                                            */
+  int64_t edges;            /* m (oriented arcs = undirected edges)                         */
+  int64_t max_out_degree;
+  int64_t wedges;           /* sum over arcs (v,u) with d(v)>=2 of d(u): the probe count     */
+  int64_t class_sizes[8];   /* vertices per schedule class (skip, g4, g8, g16, g32, warp, cta, cluster) */
+  uint64_t *vertex_cycles;  /* caller-provided device array of n entries, or NULL            */
+} trust_tc_result;
+
+typedef struct trust_tc_ctx trust_tc_ctx;
+
+/* default option values */
+void trust_tc_opts_init(trust_tc_opts *opts);
+
+/* text for a status code (static storage) */
+const char *trust_tc_strerror(int status);
+/* text of the last CUDA error seen by this thread, or "" */
+const char *trust_tc_last_cuda_error(void);
+/* library version string */
+const char *trust_tc_version(void);
+/* bytes read back from the device per counting call (status words and the count) */
+size_t trust_tc_readback_bytes(void);
+
+/* A context owns device scratch (work queues, class lists, spill tables, staging copies of
+ * host input) and reuses it across calls.  Not thread-safe; separate contexts are independent.
+ * Replaces the per-call cudaMalloc/cudaFree of Without-graph-partition/TC.cu:655-711. */
+int trust_tc_ctx_create(trust_tc_ctx **ctx, int device);
+int trust_tc_ctx_destroy(trust_tc_ctx *ctx);
+
+/* Host-side CSR check (Without-graph-partition/graph.hpp:18-67 performs none):
+ * begin[0]==0, non-decreasing, begin[n]==m, ids in [0,n), m < 2^31, out-degree < 2^26.
+ * On success writes the maximum out-degree to *max_out_degree (may be NULL). */
+int trust_tc_validate_csr(const int64_t *begin, const int32_t *adj, int64_t n, int64_t m,
+                          int64_t *max_out_degree);
+
+/* Count over a CSR.  Replaces dynamic_assign + its launch (Without-graph-partition/TC.cu:230-600,
+ * :666-696).  Arrays are borrowed; with ptr_kind HOST they are copied to ctx-owned device
+ * memory inside the call.  ctx may be NULL (a temporary context is used). */
+int trust_tc_count_csr(trust_tc_ctx *ctx, const int64_t *begin, const int32_t *adj, int64_t n,
+                       int64_t m, const trust_tc_opts *opts, trust_tc_result *result);
+
+/* Load `<folder>/begin.bin` and `<folder>/adjacent.bin` into malloc'd host arrays.
+ * Replaces graph::graph (Without-graph-partition/graph.hpp:18-67) and fsize
+ * (Without-graph-partition/comm.h:26-32): n = bytes(begin)/8 - 1, m = bytes(adj)/4, with the
+ * size checks the reference omits.  Free with trust_tc_free_host. */
+int trust_tc_load_folder(const char *folder, int64_t **begin, int32_t **adj, int64_t *n, int64_t *m);
+/* Write a CSR as begin.bin/adjacent.bin (the format Preprocess/preprocess_outdegree.cpp:205-221 writes). */
+int trust_tc_save_folder(const char *folder, const int64_t *begin, const int32_t *adj, int64_t n,
+                         int64_t m);
+void trust_tc_free_host(void *p);
+
+/* The reference operator end to end: load folder, validate, copy, count.  Replaces
+ * Triangle_count (Without-graph-partition/TC.cu:602-731). */
+int trust_tc_count_folder(const char *folder, const trust_tc_opts *opts, trust_tc_result *result);
+
+/* Partitioned operator as a one-GPU tile loop.  `folder` holds partition<i>_<j>/ tiles in the
+ * format of Preprocess/partition.cpp:72-121; all parts x parts x parts tile jobs (i,j,k) run on
+ * this GPU.  Replaces the partitioned Triangle_count (With-graph-partition/TC.cu:976-1157), which
+ * runs one (i,j,k) job per MPI rank.  For simple oriented graphs the total equals the
+ * unpartitioned count. */
+int trust_tc_count_partitioned(const char *folder, int parts, const trust_tc_opts *opts,
+                               trust_tc_result *result);
+
+/* Split a CSR into parts x parts tiles (row class v%parts, column class w%parts, local id w/parts)
+ * and write them as partition<i>_<j>/begin.bin,adjacent.bin under `folder`.  Follows
+ * Preprocess/partition.cpp:72-121 for the tile contents (map/division files are not written:
+ * the tile loop schedules rows itself). */
+int trust_tc_partition_folder(const char *folder, const int64_t *begin, const int32_t *adj,
+                              int64_t n, int64_t m, int parts);
+
+/* ---- GPU preprocessing: edge pairs -> oriented CSR -------------------------------------- */
+/* Build the oriented CSR from `npairs` (u,v) int32 pairs on the device (2*npairs ints, u at
+ * even index).  Steps: drop self-loops, symmetrise, drop duplicates, drop vertices without
+ * edges, orient each edge from lower to higher (degree, id), renumber by out-degree descending
+ * (ties by compacted id), rows sorted ascending.  Replaces Preprocess/fromDirectToUndirect.cpp
+ * :29-119 and Preprocess/preprocess_outdegree.cpp:79-222 (ties there follow std::sort order).
+ * Outputs are device arrays allocated by the library; free with trust_tc_free_device.
+ * `id_bound` is an exclusive upper bound on input ids. */
+int trust_tc_build_csr_device(trust_tc_ctx *ctx, const int32_t *d_pairs, int64_t npairs,
+                              int64_t id_bound, int64_t **d_begin, int32_t **d_adj, int64_t *n,
+                              int64_t *m);
+void trust_tc_free_device(void *p);
+/* Copy `bytes` between any two buffers the CUDA runtime can address (cudaMemcpyDefault); lets a
+ * caller that owns memory through another allocator take over library-allocated outputs. */
+int trust_tc_copy(void *dst, const void *src, size_t bytes);
+
+/* ---- deterministic synthetic graphs (counter-based RNG: identical on every host and GPU) -- */
+/* R-MAT: npairs = edge_factor << scale pairs with quadrant probabilities a,b,c (d = 1-a-b-c). */
+int trust_tc_gen_rmat_device(trust_tc_ctx *ctx, int scale, int64_t npairs, double a, double b,
+                             double c, uint64_t seed, int32_t *d_pairs);
+/* Chung-Lu: n vertices, expected degree w_i = w_max * (1 + i/i0)^(-1/(gamma-1)), i0 chosen so
+ * that sum w = 2*target_edges; draws npairs endpoint pairs proportional to w. */
+int trust_tc_gen_chung_lu_device(trust_tc_ctx *ctx, int64_t n, double gamma, double w_max,
+                                 int64_t target_edges, int64_t npairs, uint64_t seed,
+                                 int32_t *d_pairs);
+/* The Chung-Lu cumulative endpoint table used by trust_tc_gen_chung_lu_device (host, n entries,
+ * scaled to 2^63).  Returns i0. */
+double trust_tc_chung_lu_table(int64_t n, double gamma, double w_max, int64_t target_edges, uint64_t *cdf);
+/* Erdos-Renyi G(n, npairs): uniform endpoint pairs. */
+int trust_tc_gen_er_device(trust_tc_ctx *ctx, int64_t n, int64_t npairs, uint64_t seed,
+                           int32_t *d_pairs);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TRUST_TC_H */

@@ -1,0 +1,60 @@
+"""The CLI and the reference-signature operator on the GPU: same argv, same output line."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import trust_gb300 as T
+
+pytestmark = pytest.mark.gpu
+pytest.importorskip("torch")
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+CLI = os.path.join(ROOT, "trust_gb300", "trust_tc")
+GOLD = os.path.join(ROOT, "tests", "golden")
+
+
+def test_cli_line(tmp_path):
+    z = np.load(os.path.join(GOLD, "rmat_s12.npz"))
+    T.save_folder(str(tmp_path), z["ref_beg"], z["ref_adj"])
+    r = subprocess.run([CLI, str(tmp_path), "1", "1024", "1024", "1"], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
+    line = r.stdout.strip("\n")
+    assert line.endswith(" ")  # "%s,%d,%d,%lld,%f,%f \n" (Without-graph-partition/mpi_main.cpp:124)
+    folder, n, m, tri, t, teps = line.strip().split(",")
+    assert folder == str(tmp_path)
+    assert int(n) == z["ref_beg"].size - 1 and int(m) == z["ref_adj"].size
+    assert int(tri) == int(z["nx_triangles"][0])
+    assert float(t) > 0 and abs(float(teps) - int(m) / float(t) / 1e9) < 1e-3 * max(1.0, float(teps)) + 2e-6
+
+
+def test_cli_default_knobs_and_ranks(tmp_path):
+    z = np.load(os.path.join(GOLD, "k150.npz"))
+    T.save_folder(str(tmp_path), z["ref_beg"], z["ref_adj"])
+    # two logical ranks on one process: the SUM stays the whole count
+    r = subprocess.run([CLI, str(tmp_path), "2", "256", "0", "4"], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert int(r.stdout.split(",")[3]) == int(z["nx_triangles"][0])
+
+
+def test_cli_partitioned(tmp_path):
+    z = np.load(os.path.join(GOLD, "rmat_s12.npz"))
+    T.partition_folder(str(tmp_path), z["ref_beg"], z["ref_adj"], 2)
+    r = subprocess.run([CLI, str(tmp_path), "1", "1024", "1024", "1", "2"], capture_output=True, text=True,
+                       timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
+    line = r.stdout.strip().splitlines()[-1]
+    assert line.startswith(str(tmp_path) + ",triangle:")
+    assert int(line.split("triangle:")[1].split(",")[0]) == int(z["nx_triangles"][0])
+
+
+def test_python_operator(tmp_path):
+    z = np.load(os.path.join(GOLD, "chung_lu_3000.npz"))
+    T.save_folder(str(tmp_path), z["ref_beg"], z["ref_adj"])
+    a = T.Triangle_count(0, str(tmp_path), T.arguments(), 1, 1024, 1024, 1)
+    assert a.count == int(z["nx_triangles"][0])
+    assert a.edge_count == z["ref_adj"].size and a.vertices == z["ref_beg"].size - 1
+    assert a.degree == a.edge_count // a.vertices and a.time > 0
+    b = T.Triangle_count(1, str(tmp_path), T.arguments(), 2, 1024, 1024, 1)
+    assert b.count == 0 and b.edge_count == a.edge_count

@@ -1,0 +1,180 @@
+"""Parity of the sm_103a counting path with the oracle (bit-exact u64 counts).
+
+Inputs: the golden CSRs produced by the reference preprocess (unsorted rows, class layout),
+known-answer graphs, arbitrary CSRs with duplicates and self-loops (the counted quantity of
+include/trust_tc.h), and every schedule class forced through small thresholds.  Where the
+reference kernel itself (Without-graph-partition/TC.cu rebuilt for sm_103a) is available it is
+run on the same certified inputs and must agree too.
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+import trust_gb300 as T
+from trust_gb300 import _lib
+from oracle import oracle as O
+from tests import graphs
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
+
+
+def _dev(beg, adj):
+    return (torch.from_numpy(np.ascontiguousarray(beg, dtype=np.int64)).cuda(),
+            torch.from_numpy(np.ascontiguousarray(adj, dtype=np.int32)).cuda())
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    with T.Context() as c:
+        yield c
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=lambda p: os.path.basename(p)[:-4])
+def test_golden_host_and_device(ctx, path):
+    z = np.load(path)
+    expect = int(z["nx_triangles"][0])
+    beg, adj = z["ref_beg"], z["ref_adj"]
+    assert T.count_csr(beg, adj).triangles == expect
+    assert T.count_csr(beg, adj, ctx=ctx).triangles == expect
+    db, da = _dev(beg, adj)
+    r = T.count_csr(db, da, ctx=ctx)
+    assert r.triangles == expect
+    assert r.vertices == beg.size - 1 and r.edges == adj.size
+    assert r.max_out_degree == int(np.diff(beg).max())
+    assert r.wedges == O.wedges(beg, adj)
+    if "fast_beg" in z:
+        assert T.count_csr(z["fast_beg"], z["fast_adj"], ctx=ctx).triangles == expect
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=lambda p: os.path.basename(p)[:-4])
+def test_reference_kernel_agrees(path):
+    if not O.ref_kernel_available():
+        pytest.skip("reference kernel cubin not built here (oracle/build_ref.sh needs the reference sources)")
+    z = np.load(path)
+    beg, adj = z["ref_beg"], z["ref_adj"]
+    assert O.trust_check(beg, adj)[0] == O.TRUST_EXACT
+    ref, _ = O.ref_kernel_count(beg, adj, blocks=64, chunk=1)
+    assert ref == int(z["nx_triangles"][0]) == T.count_csr(beg, adj).triangles
+
+
+# (warp_max, block_max) pairs that push vertices through every class: g4..g32, warp, CTA, huge
+THRESHOLDS = [(128, 4096), (32, 32), (32, 64), (64, 128), (100, 100), (256, 8192)]
+
+
+@pytest.mark.parametrize("wm,bm", THRESHOLDS)
+@pytest.mark.parametrize("name", ["k150", "rmat_s12", "chung_lu_3000", "k60"])
+def test_every_class_path(ctx, name, wm, bm):
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", name + ".npz"))
+    db, da = _dev(z["ref_beg"], z["ref_adj"])
+    r = T.count_csr(db, da, ctx=ctx, warp_max=wm, block_max=bm)
+    assert r.triangles == int(z["nx_triangles"][0])
+    d = np.diff(z["ref_beg"])
+    cta_max = 1 << max((2 * bm - 1).bit_length() - 1, 5)  # table of the next power of two >= 2*bm
+    assert r.class_sizes["huge"] == int(np.sum(d > cta_max))
+    assert r.class_sizes["skip"] == int(np.sum(d < 2))
+
+
+@pytest.mark.parametrize("threads", [64, 128, 256, 512, 1024])
+@pytest.mark.parametrize("blocks,chunk", [(0, 0), (1, 1), (7, 3), (300, 16)])
+def test_launch_shapes(ctx, threads, blocks, chunk):
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "rmat_s12.npz"))
+    db, da = _dev(z["ref_beg"], z["ref_adj"])
+    r = T.count_csr(db, da, ctx=ctx, threads=threads, blocks=blocks, chunk=chunk, warp_max=64, block_max=256)
+    assert r.triangles == int(z["nx_triangles"][0])
+
+
+@pytest.mark.parametrize("name,pairs,tri", graphs.kat_cases(), ids=[c[0] for c in graphs.kat_cases()])
+def test_known_answers(ctx, name, pairs, tri):
+    beg, adj = O.build_csr(pairs, int(pairs.max()) + 1)
+    assert T.count_csr(beg, adj, ctx=ctx).triangles == tri
+    assert T.count_csr(beg, adj, ctx=ctx, warp_max=32, block_max=32).triangles == tri
+
+
+def test_arbitrary_csr_formula(ctx):
+    """Unsorted rows, duplicate arcs, self-loops: the counted quantity, not just triangles."""
+    rng = np.random.default_rng(1)
+    for trial in range(40):
+        n = int(rng.integers(1, 400))
+        beg, adj = graphs.random_csr(rng, n, int(rng.integers(0, 40)))
+        expect = O.count_forward(beg, adj)
+        db, da = _dev(beg, adj)
+        for wm, bm in ((128, 4096), (32, 32)):
+            assert T.count_csr(db, da, ctx=ctx, warp_max=wm, block_max=bm).triangles == expect
+
+
+def test_edge_cases(ctx):
+    assert T.count_csr(np.array([0]), np.array([], dtype=np.int32), ctx=ctx).triangles == 0
+    assert T.count_csr(np.array([0, 0]), np.array([], dtype=np.int32), ctx=ctx).triangles == 0
+    # every out-degree < 2
+    beg = np.array([0, 1, 2, 2], dtype=np.int64)
+    adj = np.array([1, 2], dtype=np.int32)
+    assert T.count_csr(beg, adj, ctx=ctx).triangles == 0
+    # a single vertex with a self-loop twice: row {0, 0}; d=2 -> each arc probes row 0 (2 entries, both hit)
+    assert T.count_csr(np.array([0, 2]), np.array([0, 0], dtype=np.int32), ctx=ctx).triangles == 4
+    db, da = _dev(np.array([0]), np.zeros(0, dtype=np.int32))
+    assert T.count_csr(db, da, ctx=ctx).triangles == 0
+
+
+def test_host_input_validation_errors(ctx):
+    beg = np.array([0, 2, 3, 3], dtype=np.int64)
+    for adj, code in (([1, 7, 2], _lib.E_IDS), ([1, -1, 2], _lib.E_IDS)):
+        with pytest.raises(T.TrustTcError) as e:
+            T.count_csr(beg, np.array(adj, dtype=np.int32), ctx=ctx)
+        assert e.value.status == code
+    for b in ([0, 2, 1, 3], [1, 2, 3, 3], [0, 2, 3, 4]):
+        with pytest.raises(T.TrustTcError) as e:
+            T.count_csr(np.array(b), np.array([1, 2, 2], dtype=np.int32), ctx=ctx)
+        assert e.value.status == _lib.E_OFFSETS
+
+
+def test_device_validation_errors(ctx):
+    db, da = _dev(np.array([0, 2, 3, 3]), np.array([1, 3, 2]))
+    with pytest.raises(T.TrustTcError) as e:
+        T.count_csr(db, da, ctx=ctx)
+    assert e.value.status == _lib.E_IDS
+    db, da = _dev(np.array([0, 2, 1, 3]), np.array([1, 2, 2]))
+    with pytest.raises(T.TrustTcError) as e:
+        T.count_csr(db, da, ctx=ctx)
+    assert e.value.status == _lib.E_OFFSETS
+    db, da = _dev(np.array([0, 2, 3, 4]), np.array([1, 2, 2]))
+    with pytest.raises(T.TrustTcError) as e:
+        T.count_csr(db, da, ctx=ctx)
+    assert e.value.status == _lib.E_OFFSETS
+    # the context is still usable afterwards
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "k60.npz"))
+    assert T.count_csr(*_dev(z["ref_beg"], z["ref_adj"]), ctx=ctx).triangles == int(z["nx_triangles"][0])
+
+
+def test_stream_and_context_reuse(ctx):
+    s = torch.cuda.Stream()
+    zs = [np.load(p) for p in GOLDEN]
+    with torch.cuda.stream(s):
+        for z in zs + zs[::-1]:
+            db, da = _dev(z["ref_beg"], z["ref_adj"])
+            r = T.count_csr(db, da, ctx=ctx, stream=s.cuda_stream)
+            assert r.triangles == int(z["nx_triangles"][0])
+            assert 0 < r.count_seconds <= r.kernel_seconds <= r.call_seconds
+
+
+def test_relabelled_input(ctx):
+    """Count is invariant under a random vertex relabelling with shuffled rows (no class layout)."""
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "rmat_s12.npz"))
+    beg, adj = z["ref_beg"], z["ref_adj"]
+    n = beg.size - 1
+    rng = np.random.default_rng(5)
+    perm = rng.permutation(n).astype(np.int32)
+    rows = [perm[adj[beg[v]:beg[v + 1]]] for v in range(n)]
+    new_rows = [None] * n
+    for v in range(n):
+        r = rows[v].copy()
+        rng.shuffle(r)
+        new_rows[perm[v]] = r
+    nb = np.zeros(n + 1, dtype=np.int64)
+    nb[1:] = np.cumsum([len(r) for r in new_rows])
+    na = np.concatenate(new_rows).astype(np.int32)
+    assert T.count_csr(nb, na, ctx=ctx).triangles == int(z["nx_triangles"][0])

@@ -1,0 +1,249 @@
+"""trust_gb300 — GB300-native (sm_103a) vertex-centric hash triangle counter.
+
+Python host mirror of TRUST's operator surface over the C ABI of include/trust_tc.h:
+
+  Triangle_count(rank, name, args, total_process, n_threads, n_blocks, chunk_size[, partition_num])
+      the reference operator (Without-graph-partition/TC.cu:602-731 and
+      With-graph-partition/TC.cu:976-1157), returning the same `arguments` record
+      (Without-graph-partition/TC.cuh:2-8)
+  count_csr / count_folder / count_partitioned
+      the C entry points with numpy (host) or torch CUDA (device) arrays
+  gen_rmat / gen_chung_lu / gen_er / build_csr
+      deterministic synthetic graphs and the GPU preprocessing into an oriented CSR
+
+Every count runs in libtrust_tc.so on the GPU; a missing library or device raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib
+from ._lib import (CLASS_NAMES, DEVICE, HOST, SCHED_LEARNED, SCHED_PLAIN, VALIDATE_FULL, VALIDATE_NONE,
+                   VALIDATE_OFFSETS, TrustTcError, check, load)
+
+__all__ = [
+    "arguments", "Triangle_count", "Context", "CountResult", "count_csr", "count_folder", "count_partitioned",
+    "load_folder", "save_folder", "partition_folder", "gen_rmat", "gen_chung_lu", "gen_er", "build_csr",
+    "chung_lu_table", "TrustTcError", "load",
+]
+
+
+@dataclass
+class arguments:  # noqa: N801 — the reference's name (Without-graph-partition/TC.cuh:2-8)
+    edge_count: int = 0
+    count: int = 0
+    time: float = 0.0
+    degree: int = 0
+    vertices: int = 0
+
+
+@dataclass
+class CountResult:
+    triangles: int
+    kernel_seconds: float
+    count_seconds: float
+    call_seconds: float
+    vertices: int
+    edges: int
+    max_out_degree: int
+    class_sizes: dict = field(default_factory=dict)
+
+
+def _result(r: _lib.Result) -> CountResult:
+    return CountResult(int(r.triangles), r.kernel_seconds, r.count_seconds, r.call_seconds, int(r.vertices),
+                       int(r.edges), int(r.max_out_degree),
+                       {k: int(v) for k, v in zip(CLASS_NAMES, r.class_sizes)})
+
+
+def _opts(threads=0, blocks=0, chunk=0, ptr_kind=HOST, validate=VALIDATE_FULL, warp_max=0, block_max=0,
+          stream=None, device=-1, schedule=SCHED_PLAIN) -> _lib.Opts:
+    o = _lib.Opts()
+    load().trust_tc_opts_init(C.byref(o))
+    o.device = device
+    o.threads_per_block = threads
+    o.blocks = blocks
+    o.chunk = chunk
+    o.ptr_kind = ptr_kind
+    o.validate = validate
+    o.warp_max_degree = warp_max
+    o.block_max_degree = block_max
+    o.schedule = schedule
+    o.stream = stream
+    return o
+
+
+class Context:
+    """Reusable device scratch (trust_tc_ctx).  Use as a context manager or call close()."""
+
+    def __init__(self, device: int = -1):
+        h = C.c_void_p()
+        check(load().trust_tc_ctx_create(C.byref(h), device), "trust_tc_ctx_create")
+        self.handle = h
+
+    def close(self) -> None:
+        if self.handle:
+            load().trust_tc_ctx_destroy(self.handle)
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _is_torch_cuda(x) -> bool:
+    return type(x).__module__.startswith("torch") and getattr(x, "is_cuda", False)
+
+
+def count_csr(beg, adj, *, ctx: Context | None = None, threads=0, blocks=0, chunk=0, stream=None,
+              validate=VALIDATE_FULL, warp_max=0, block_max=0) -> CountResult:
+    """Count over a CSR held in numpy arrays (host) or contiguous torch CUDA tensors (device).
+
+    `stream` is a cudaStream_t value (e.g. torch.cuda.current_stream().cuda_stream)."""
+    lib = load()
+    if _is_torch_cuda(beg):
+        import torch
+        assert beg.dtype == torch.int64 and adj.dtype == torch.int32 and beg.is_contiguous() and adj.is_contiguous()
+        n, m = beg.numel() - 1, adj.numel()
+        pb, pa, kind = C.c_void_p(beg.data_ptr()), C.c_void_p(adj.data_ptr() if m else 0), DEVICE
+        keep = (beg, adj)
+    else:
+        b = np.ascontiguousarray(beg, dtype=np.int64)
+        a = np.ascontiguousarray(adj, dtype=np.int32)
+        n, m = b.size - 1, a.size
+        pb, pa, kind = b.ctypes.data_as(C.c_void_p), a.ctypes.data_as(C.c_void_p), HOST
+        keep = (b, a)
+    o = _opts(threads, blocks, chunk, kind, validate, warp_max, block_max, stream)
+    r = _lib.Result()
+    st = lib.trust_tc_count_csr(ctx.handle if ctx else None, pb, pa, n, m, C.byref(o), C.byref(r))
+    del keep
+    check(st, "trust_tc_count_csr")
+    return _result(r)
+
+
+def count_folder(folder: str, threads=0, blocks=0, chunk=0) -> CountResult:
+    o = _opts(threads, blocks, chunk)
+    r = _lib.Result()
+    check(load().trust_tc_count_folder(folder.encode(), C.byref(o), C.byref(r)), "trust_tc_count_folder")
+    return _result(r)
+
+
+def count_partitioned(folder: str, parts: int, threads=0, blocks=0, chunk=0) -> CountResult:
+    o = _opts(threads, blocks, chunk)
+    r = _lib.Result()
+    check(load().trust_tc_count_partitioned(folder.encode(), parts, C.byref(o), C.byref(r)),
+          "trust_tc_count_partitioned")
+    return _result(r)
+
+
+def Triangle_count(rank: int, name: str, args: arguments, total_process: int, n_threads: int, n_blocks: int,
+                   chunk_size: int, partition_num: int | None = None) -> arguments:  # noqa: N802
+    """The reference operator.  One GPU: rank 0 returns the whole count, other ranks 0, so the
+    caller's SUM over ranks (Without-graph-partition/mpi_main.cpp:119) is unchanged.  Where the
+    reference prints and exits on error, this raises TrustTcError."""
+    del total_process
+    if rank > 0:
+        if partition_num is None:
+            b, a = load_folder(name)
+            return arguments(edge_count=a.size, count=0, time=0.0,
+                             degree=(a.size // (b.size - 1)) if b.size > 1 else 0, vertices=b.size - 1)
+        return arguments()
+    if partition_num is None:
+        r = count_folder(name, n_threads, n_blocks, chunk_size)
+    else:
+        r = count_partitioned(name, partition_num, n_threads, n_blocks, chunk_size)
+    return arguments(edge_count=r.edges, count=r.triangles, time=r.kernel_seconds,
+                     degree=(r.edges // r.vertices) if r.vertices else 0, vertices=r.vertices)
+
+
+def load_folder(folder: str):
+    lib = load()
+    pb, pa = C.POINTER(C.c_int64)(), C.POINTER(C.c_int32)()
+    n, m = C.c_int64(), C.c_int64()
+    check(lib.trust_tc_load_folder(folder.encode(), C.byref(pb), C.byref(pa), C.byref(n), C.byref(m)),
+          "trust_tc_load_folder")
+    try:
+        beg = np.ctypeslib.as_array(pb, shape=(n.value + 1,)).copy()
+        adj = np.ctypeslib.as_array(pa, shape=(max(m.value, 1),))[: m.value].copy()
+    finally:
+        lib.trust_tc_free_host(C.cast(pb, C.c_void_p))
+        lib.trust_tc_free_host(C.cast(pa, C.c_void_p))
+    return beg, adj
+
+
+def save_folder(folder: str, beg, adj) -> None:
+    b = np.ascontiguousarray(beg, dtype=np.int64)
+    a = np.ascontiguousarray(adj, dtype=np.int32)
+    check(load().trust_tc_save_folder(folder.encode(), b.ctypes.data_as(C.c_void_p), a.ctypes.data_as(C.c_void_p),
+                                      b.size - 1, a.size), "trust_tc_save_folder")
+
+
+def partition_folder(folder: str, beg, adj, parts: int) -> None:
+    b = np.ascontiguousarray(beg, dtype=np.int64)
+    a = np.ascontiguousarray(adj, dtype=np.int32)
+    check(load().trust_tc_partition_folder(folder.encode(), b.ctypes.data_as(C.c_void_p),
+                                           a.ctypes.data_as(C.c_void_p), b.size - 1, a.size, parts),
+          "trust_tc_partition_folder")
+
+
+def chung_lu_table(n: int, gamma: float, w_max: float, target_edges: int) -> np.ndarray:
+    cdf = np.zeros(n, dtype=np.uint64)
+    load().trust_tc_chung_lu_table(n, gamma, w_max, target_edges, cdf.ctypes.data_as(C.c_void_p))
+    return cdf
+
+
+def _pairs(npairs: int):
+    import torch
+    return torch.empty((npairs, 2), dtype=torch.int32, device="cuda")
+
+
+def gen_rmat(scale: int, edge_factor: int, a=0.57, b=0.19, c=0.19, seed=1, npairs: int | None = None):
+    """R-MAT pairs on the GPU: (edge_factor << scale) x 2 int32 tensor."""
+    np_ = (edge_factor << scale) if npairs is None else npairs
+    out = _pairs(np_)
+    check(load().trust_tc_gen_rmat_device(None, scale, np_, a, b, c, seed, C.c_void_p(out.data_ptr())),
+          "trust_tc_gen_rmat_device")
+    return out
+
+
+def gen_chung_lu(n: int, gamma: float, w_max: float, target_edges: int, npairs: int, seed=2):
+    out = _pairs(npairs)
+    check(load().trust_tc_gen_chung_lu_device(None, n, gamma, w_max, target_edges, npairs, seed,
+                                              C.c_void_p(out.data_ptr())), "trust_tc_gen_chung_lu_device")
+    return out
+
+
+def gen_er(n: int, npairs: int, seed=5):
+    out = _pairs(npairs)
+    check(load().trust_tc_gen_er_device(None, n, npairs, seed, C.c_void_p(out.data_ptr())), "trust_tc_gen_er_device")
+    return out
+
+
+def build_csr(pairs, id_bound: int):
+    """GPU preprocessing of an (npairs, 2) int32 CUDA tensor into an oriented CSR (beg int64, adj int32)."""
+    import torch
+    lib = load()
+    pb, pa = C.c_void_p(), C.c_void_p()
+    n, m = C.c_int64(), C.c_int64()
+    pairs = pairs.contiguous()
+    check(lib.trust_tc_build_csr_device(None, C.c_void_p(pairs.data_ptr()), pairs.shape[0], id_bound, C.byref(pb),
+                                        C.byref(pa), C.byref(n), C.byref(m)), "trust_tc_build_csr_device")
+    try:
+        beg = torch.empty(n.value + 1, dtype=torch.int64, device="cuda")
+        adj = torch.empty(max(m.value, 1), dtype=torch.int32, device="cuda")
+        check(lib.trust_tc_copy(C.c_void_p(beg.data_ptr()), pb, 8 * (n.value + 1)), "trust_tc_copy")
+        check(lib.trust_tc_copy(C.c_void_p(adj.data_ptr()), pa, 4 * m.value), "trust_tc_copy")
+    finally:
+        lib.trust_tc_free_device(pb)
+        lib.trust_tc_free_device(pa)
+    return beg, adj[: m.value]

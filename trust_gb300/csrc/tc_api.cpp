@@ -1,0 +1,406 @@
+// tc_api.cpp — C ABI of the counter: contexts, validation, folder I/O, the count call.
+//
+// Host operator that replaces Triangle_count (Without-graph-partition/TC.cu:602-731): it loads
+// the CSR (graph::graph, Without-graph-partition/graph.hpp:18-67), checks it, copies it to the
+// device, classifies vertices (the degree split of TC.cu:632, generalised), launches the
+// persistent counting kernel and reads the u64 count back.  Unlike the reference it validates
+// input, never exits, reuses device scratch across calls through a context, and times the
+// kernels with CUDA events instead of process CPU time (TC.cu:686-692).
+#include <cuda_runtime.h>
+#include <errno.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <sys/stat.h>
+
+#include <algorithm>
+#include <string>
+
+#include "tc_count.h"
+#include "tc_internal.h"
+
+namespace tc {
+
+static thread_local char g_cuda_err[256] = "";
+
+int cuda_status(cudaError_t e) {
+  if (e == cudaSuccess) return TRUST_TC_OK;
+  snprintf(g_cuda_err, sizeof g_cuda_err, "%s (%s)", cudaGetErrorString(e), cudaGetErrorName(e));
+  if (e == cudaErrorMemoryAllocation) return TRUST_TC_E_NOMEM;
+  if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return TRUST_TC_E_NO_DEVICE;
+  return TRUST_TC_E_CUDA;
+}
+
+int ctx_init(trust_tc_ctx *c, int device) {
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0) {
+    if (e != cudaSuccess) cuda_status(e);
+    return TRUST_TC_E_NO_DEVICE;
+  }
+  if (device < 0) TC_CUDA_TRY(cudaGetDevice(&device));
+  if (device >= ndev) return TRUST_TC_E_ARG;
+  TC_CUDA_TRY(cudaSetDevice(device));
+  c->device = device;
+  TC_CUDA_TRY(cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device));
+  TC_CUDA_TRY(cudaDeviceGetAttribute(&c->max_smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device));
+  TC_CUDA_TRY(cudaMalloc(&c->d_ctl, sizeof(TcControl)));
+  TC_CUDA_TRY(cudaMallocHost(&c->h_ctl, sizeof(TcControl)));
+  for (auto &ev : c->ev) TC_CUDA_TRY(cudaEventCreate(&ev));
+  return TRUST_TC_OK;
+}
+
+void ctx_release(trust_tc_ctx *c) {
+  if (c->device >= 0) cudaSetDevice(c->device);
+  cudaFree(c->d_ctl);
+  cudaFreeHost(c->h_ctl);
+  cudaFree(c->d_lists);
+  cudaFree(c->d_huge);
+  cudaFree(c->d_beg);
+  cudaFree(c->d_adj);
+  for (auto &ev : c->ev)
+    if (ev) cudaEventDestroy(ev);
+  *c = trust_tc_ctx();
+}
+
+// Grow a device buffer to at least `bytes` (contents are not kept).
+int ensure(void **p, size_t *cap, size_t bytes) {
+  if (*cap >= bytes && *p) return TRUST_TC_OK;
+  if (*p) cudaFree(*p);
+  *p = nullptr;
+  *cap = 0;
+  size_t want = std::max<size_t>(bytes, 256);
+  TC_CUDA_TRY(cudaMalloc(p, want));
+  *cap = want;
+  return TRUST_TC_OK;
+}
+
+static int ceil_log2_size(int64_t x) {
+  int l = 0;
+  while (((int64_t)1 << l) < x) ++l;
+  return l;
+}
+
+// Resolved launch configuration for one counting call.
+struct LaunchCfg {
+  int threads, blocks, chunk, warp_max, cta_max, cta_log2, warp_slots;
+  size_t smem;
+};
+
+static int resolve_cfg(trust_tc_ctx *c, const trust_tc_opts &o, bool same, LaunchCfg *cfg) {
+  cfg->threads = o.threads_per_block > 0 ? o.threads_per_block : 256;
+  if (cfg->threads % 32 || cfg->threads < 64 || cfg->threads > 1024) return TRUST_TC_E_ARG;
+  cfg->warp_max = o.warp_max_degree > 0 ? o.warp_max_degree : 128;
+  if (cfg->warp_max < 32 || cfg->warp_max > 4096) return TRUST_TC_E_ARG;
+  int want_cta = o.block_max_degree > 0 ? o.block_max_degree : 4096;
+  if (want_cta < cfg->warp_max) return TRUST_TC_E_ARG;
+  cfg->cta_log2 = std::max(ceil_log2_size(2 * (int64_t)want_cta), 6);
+  const int warps = cfg->threads / 32;
+  cfg->warp_slots = 1 << std::max(ceil_log2_size(2 * (int64_t)cfg->warp_max), 7);  // >= 4*32 for G32 groups
+  size_t table_bytes = (size_t)4 << cfg->cta_log2;
+  size_t warp_bytes = (size_t)4 * cfg->warp_slots * warps;
+  cfg->smem = std::max(table_bytes, warp_bytes);
+  if (cfg->smem > (size_t)c->max_smem_optin) return TRUST_TC_E_ARG;
+  cfg->cta_max = 1 << (cfg->cta_log2 - 1);
+  cfg->chunk = o.chunk > 0 ? o.chunk : 4;
+  int per_sm = 0;
+  int st = count_kernel_occupancy(same, cfg->threads, cfg->smem, &per_sm);
+  if (st) return st;
+  if (per_sm < 1) return TRUST_TC_E_ARG;
+  cfg->blocks = o.blocks > 0 ? o.blocks : c->num_sms * per_sm;
+  return TRUST_TC_OK;
+}
+
+// The device-side counting call over three CSRs (A = tables, B = arcs, C = probe lists).
+// `check_*` select which CSRs get an id-range check on the device.
+int count_device(trust_tc_ctx *c, const DevGraph3 &g, const trust_tc_opts &o, bool check_ids,
+                 trust_tc_result *r) {
+  cudaStream_t st = (cudaStream_t)o.stream;
+  const bool same = g.begA == g.begB && g.begB == g.begC && g.adjA == g.adjB && g.adjB == g.adjC;
+  LaunchCfg cfg;
+  int rc = resolve_cfg(c, o, same, &cfg);
+  if (rc) return rc;
+  TcControl *ctl = c->d_ctl;
+  TC_CUDA_TRY(cudaEventRecord(c->ev[0], st));
+  TC_CUDA_TRY(cudaMemsetAsync(ctl, 0, sizeof(TcControl), st));
+  // 1. validation of every distinct CSR: offsets always, ids on request
+  rc = launch_check(g.begA, g.adjA, g.rows, g.mA, g.boundA, check_ids, ctl, c->num_sms, st);
+  if (rc) return rc;
+  if (!same) {
+    rc = launch_check(g.begB, g.adjB, g.rows, g.mB, g.boundB, check_ids, ctl, c->num_sms, st);
+    if (rc) return rc;
+    rc = launch_check(g.begC, g.adjC, g.rowsC, g.mC, g.boundC, check_ids, ctl, c->num_sms, st);
+    if (rc) return rc;
+  }
+  // 2. classification histogram
+  TC_CUDA_TRY(cudaEventRecord(c->ev[1], st));
+  ListOffsets off{};
+  rc = launch_classify(0, g.begA, g.begB, g.rows, g.min_deg, cfg.warp_max, cfg.cta_max, ctl, c->d_lists,
+                       off, c->num_sms, st);
+  if (rc) return rc;
+  TC_CUDA_TRY(cudaMemcpyAsync(c->h_ctl, ctl, sizeof(TcControl), cudaMemcpyDeviceToHost, st));
+  TC_CUDA_TRY(cudaStreamSynchronize(st));
+  const TcControl h = *c->h_ctl;
+  if (h.status & TC_DEV_BAD_OFFSETS) return TRUST_TC_E_OFFSETS;
+  if (h.status & TC_DEV_TOO_LARGE) return TRUST_TC_E_TOO_LARGE;
+  if (h.status & TC_DEV_BAD_IDS) return TRUST_TC_E_IDS;
+  int64_t total = 0;
+  for (int k = TC_CLASS_SKIP + 1; k < TC_NUM_CLASSES; ++k) {
+    off.off[k] = (int)total;
+    total += h.class_count[k];
+  }
+  rc = ensure((void **)&c->d_lists, &c->lists_cap, (size_t)std::max<int64_t>(total, 1) * sizeof(int));
+  if (rc) return rc;
+  // huge class: one global table per participating CTA, 2x the largest list
+  CountArgs a{};
+  if (h.class_count[TC_CLASS_HUGE] > 0) {
+    a.huge_log2 = ceil_log2_size(2 * (int64_t)h.max_out_degree);
+    size_t per = (size_t)4 << a.huge_log2;
+    size_t budget = (size_t)1 << 31;  // 2 GiB of spill tables at most
+    int nb = (int)std::min<size_t>(std::max<size_t>(budget / per, 1), (size_t)cfg.blocks);
+    nb = std::min(nb, h.class_count[TC_CLASS_HUGE]);
+    a.huge_blocks = nb;
+    rc = ensure((void **)&c->d_huge, &c->huge_cap, per * nb);
+    if (rc) return rc;
+  }
+  // 3. scatter the class lists
+  rc = launch_classify(1, g.begA, g.begB, g.rows, g.min_deg, cfg.warp_max, cfg.cta_max, ctl, c->d_lists,
+                       off, c->num_sms, st);
+  if (rc) return rc;
+  // 4. count
+  a.begA = g.begA; a.begB = g.begB; a.begC = g.begC;
+  a.adjA = g.adjA; a.adjB = g.adjB; a.adjC = g.adjC;
+  a.rows = g.rows;
+  a.lists = c->d_lists;
+  a.off = off;
+  a.ctl = ctl;
+  a.huge_tables = c->d_huge;
+  a.warp_slots = cfg.warp_slots;
+  a.chunk = cfg.chunk;
+  TC_CUDA_TRY(cudaEventRecord(c->ev[2], st));
+  rc = launch_count(same, a, cfg.blocks, cfg.threads, cfg.smem, st);
+  if (rc) return rc;
+  TC_CUDA_TRY(cudaEventRecord(c->ev[3], st));
+  TC_CUDA_TRY(cudaMemcpyAsync(c->h_ctl, ctl, sizeof(TcControl), cudaMemcpyDeviceToHost, st));
+  TC_CUDA_TRY(cudaEventRecord(c->ev[4], st));
+  TC_CUDA_TRY(cudaStreamSynchronize(st));
+  const TcControl done = *c->h_ctl;
+  if (done.status & TC_DEV_TABLE_FULL) return TRUST_TC_E_DEVICE;
+  float t_kernel = 0, t_count = 0, t_call = 0;
+  TC_CUDA_TRY(cudaEventElapsedTime(&t_kernel, c->ev[1], c->ev[3]));
+  TC_CUDA_TRY(cudaEventElapsedTime(&t_count, c->ev[2], c->ev[3]));
+  TC_CUDA_TRY(cudaEventElapsedTime(&t_call, c->ev[0], c->ev[4]));
+  r->triangles = done.count;
+  r->wedges = (int64_t)done.wedges;
+  r->kernel_seconds = t_kernel * 1e-3;
+  r->count_seconds = t_count * 1e-3;
+  r->call_seconds = t_call * 1e-3;
+  r->max_out_degree = done.max_out_degree;
+  for (int k = 0; k < TC_NUM_CLASSES; ++k) r->class_sizes[k] = h.class_count[k];
+  return TRUST_TC_OK;
+}
+
+}  // namespace tc
+
+using namespace tc;
+
+// ------------------------------------------------------------------------------------------
+// C ABI
+// ------------------------------------------------------------------------------------------
+extern "C" {
+
+void trust_tc_opts_init(trust_tc_opts *o) {
+  if (!o) return;
+  memset(o, 0, sizeof *o);
+  o->device = -1;
+  o->ptr_kind = TRUST_TC_HOST;
+  o->schedule = TRUST_TC_SCHED_PLAIN;
+  o->validate = TRUST_TC_VALIDATE_FULL;
+}
+
+const char *trust_tc_strerror(int s) {
+  switch (s) {
+    case TRUST_TC_OK: return "ok";
+    case TRUST_TC_E_ARG: return "invalid argument";
+    case TRUST_TC_E_IO: return "cannot read or write graph files";
+    case TRUST_TC_E_FORMAT: return "graph file sizes are not whole records";
+    case TRUST_TC_E_OFFSETS: return "begin offsets are not a valid CSR (begin[0]!=0, decreasing, or begin[n]!=m)";
+    case TRUST_TC_E_IDS: return "a neighbour id is outside [0, n)";
+    case TRUST_TC_E_TOO_LARGE: return "graph exceeds limits (m or n >= 2^31, or an out-degree >= 2^26)";
+    case TRUST_TC_E_CUDA: return "CUDA runtime error";
+    case TRUST_TC_E_NOMEM: return "out of memory";
+    case TRUST_TC_E_DEVICE: return "device-side error (table overflow or bounded wait expired)";
+    case TRUST_TC_E_UNSUPPORTED: return "unsupported option combination";
+    case TRUST_TC_E_NO_DEVICE: return "no CUDA device available";
+    default: return "unknown status";
+  }
+}
+
+const char *trust_tc_last_cuda_error(void) { return g_cuda_err; }
+
+const char *trust_tc_version(void) { return "trust-gb300 0.1 (sm_103a)"; }
+
+size_t trust_tc_readback_bytes(void) { return 2 * sizeof(TcControl); }
+
+int trust_tc_ctx_create(trust_tc_ctx **out, int device) {
+  if (!out) return TRUST_TC_E_ARG;
+  *out = nullptr;
+  trust_tc_ctx *c = new (std::nothrow) trust_tc_ctx();
+  if (!c) return TRUST_TC_E_NOMEM;
+  int rc = ctx_init(c, device);
+  if (rc) {
+    ctx_release(c);
+    delete c;
+    return rc;
+  }
+  *out = c;
+  return TRUST_TC_OK;
+}
+
+int trust_tc_ctx_destroy(trust_tc_ctx *c) {
+  if (!c) return TRUST_TC_E_ARG;
+  ctx_release(c);
+  delete c;
+  return TRUST_TC_OK;
+}
+
+int trust_tc_validate_csr(const int64_t *beg, const int32_t *adj, int64_t n, int64_t m,
+                          int64_t *max_out_degree) {
+  if (!beg || n < 0 || m < 0 || (m > 0 && !adj)) return TRUST_TC_E_ARG;
+  if (n >= ((int64_t)1 << 31) || m >= ((int64_t)1 << 31)) return TRUST_TC_E_TOO_LARGE;
+  if (beg[0] != 0 || beg[n] != m) return TRUST_TC_E_OFFSETS;
+  int64_t dmax = 0;
+  for (int64_t v = 0; v < n; ++v) {
+    int64_t d = beg[v + 1] - beg[v];
+    if (d < 0) return TRUST_TC_E_OFFSETS;
+    if (d >= ((int64_t)1 << 26)) return TRUST_TC_E_TOO_LARGE;
+    dmax = std::max(dmax, d);
+  }
+  for (int64_t i = 0; i < m; ++i)
+    if (adj[i] < 0 || (int64_t)adj[i] >= n) return TRUST_TC_E_IDS;
+  if (max_out_degree) *max_out_degree = dmax;
+  return TRUST_TC_OK;
+}
+
+int trust_tc_count_csr(trust_tc_ctx *ctx, const int64_t *beg, const int32_t *adj, int64_t n, int64_t m,
+                       const trust_tc_opts *opts, trust_tc_result *r) {
+  if (!beg || !r || n < 0 || m < 0 || (m > 0 && !adj)) return TRUST_TC_E_ARG;
+  trust_tc_opts o;
+  if (opts) o = *opts; else trust_tc_opts_init(&o);
+  if (o.ptr_kind != TRUST_TC_HOST && o.ptr_kind != TRUST_TC_DEVICE) return TRUST_TC_E_ARG;
+  if (o.schedule != TRUST_TC_SCHED_PLAIN && o.schedule != TRUST_TC_SCHED_LEARNED) return TRUST_TC_E_ARG;
+  if (n >= ((int64_t)1 << 31) || m >= ((int64_t)1 << 31)) return TRUST_TC_E_TOO_LARGE;
+  uint64_t *cycles = r->vertex_cycles;
+  memset(r, 0, sizeof *r);
+  r->vertex_cycles = cycles;
+  r->vertices = n;
+  r->edges = m;
+  int rc;
+  trust_tc_ctx tmp;
+  trust_tc_ctx *c = ctx;
+  if (!c) {
+    rc = ctx_init(&tmp, o.device);
+    if (rc) { ctx_release(&tmp); return rc; }
+    c = &tmp;
+  } else if (o.device >= 0 && o.device != c->device) {
+    return TRUST_TC_E_ARG;
+  }
+  if ((rc = cuda_status(cudaSetDevice(c->device)))) { if (c == &tmp) ctx_release(&tmp); return rc; }
+  DevGraph3 g{};
+  bool check_ids = false;
+  if (o.ptr_kind == TRUST_TC_HOST) {
+    rc = ensure((void **)&c->d_beg, &c->beg_cap, sizeof(int64_t) * (size_t)(n + 1));
+    if (!rc) rc = ensure((void **)&c->d_adj, &c->adj_cap, sizeof(int32_t) * (size_t)std::max<int64_t>(m, 1));
+    cudaStream_t st = (cudaStream_t)o.stream;
+    if (!rc) rc = cuda_status(cudaMemcpyAsync(c->d_beg, beg, sizeof(int64_t) * (size_t)(n + 1), cudaMemcpyHostToDevice, st));
+    if (!rc && m) rc = cuda_status(cudaMemcpyAsync(c->d_adj, adj, sizeof(int32_t) * (size_t)m, cudaMemcpyHostToDevice, st));
+    g.begA = g.begB = g.begC = c->d_beg;
+    g.adjA = g.adjB = g.adjC = c->d_adj;
+    check_ids = true;  // host input is checked on the device after the copy, never skipped
+  } else {
+    g.begA = g.begB = g.begC = beg;
+    g.adjA = g.adjB = g.adjC = adj;
+    check_ids = o.validate >= TRUST_TC_VALIDATE_FULL;
+  }
+  if (!rc) {
+    g.rows = g.rowsC = n;
+    g.mA = g.mB = g.mC = m;
+    g.boundA = g.boundB = g.boundC = n;
+    g.min_deg = 2;
+    rc = count_device(c, g, o, check_ids, r);
+  }
+  r->vertices = n;
+  r->edges = m;
+  if (c == &tmp) ctx_release(&tmp);
+  return rc;
+}
+
+void trust_tc_free_host(void *p) { free(p); }
+
+static int64_t file_bytes(const std::string &path) {
+  struct stat st;
+  if (stat(path.c_str(), &st) != 0) return -1;
+  return (int64_t)st.st_size;
+}
+
+static int read_all(const std::string &path, void *dst, size_t bytes) {
+  FILE *f = fopen(path.c_str(), "rb");
+  if (!f) return TRUST_TC_E_IO;
+  size_t got = bytes ? fread(dst, 1, bytes, f) : 0;
+  fclose(f);
+  return got == bytes ? TRUST_TC_OK : TRUST_TC_E_IO;
+}
+
+int trust_tc_load_folder(const char *folder, int64_t **beg, int32_t **adj, int64_t *n, int64_t *m) {
+  if (!folder || !beg || !adj || !n || !m) return TRUST_TC_E_ARG;
+  *beg = nullptr;
+  *adj = nullptr;
+  std::string fb = std::string(folder) + "/begin.bin", fa = std::string(folder) + "/adjacent.bin";
+  int64_t bb = file_bytes(fb), ab = file_bytes(fa);
+  if (bb < 0 || ab < 0) return TRUST_TC_E_IO;
+  if (bb < 8 || bb % 8 || ab % 4) return TRUST_TC_E_FORMAT;
+  int64_t nn = bb / 8 - 1, mm = ab / 4;
+  if (nn >= ((int64_t)1 << 31) || mm >= ((int64_t)1 << 31)) return TRUST_TC_E_TOO_LARGE;
+  int64_t *b = (int64_t *)malloc((size_t)bb);
+  int32_t *a = (int32_t *)malloc((size_t)std::max<int64_t>(ab, 4));
+  if (!b || !a) { free(b); free(a); return TRUST_TC_E_NOMEM; }
+  int rc = read_all(fb, b, (size_t)bb);
+  if (!rc) rc = read_all(fa, a, (size_t)ab);
+  if (rc) { free(b); free(a); return rc; }
+  *beg = b;
+  *adj = a;
+  *n = nn;
+  *m = mm;
+  return TRUST_TC_OK;
+}
+
+int trust_tc_save_folder(const char *folder, const int64_t *beg, const int32_t *adj, int64_t n, int64_t m) {
+  if (!folder || !beg || n < 0 || m < 0 || (m && !adj)) return TRUST_TC_E_ARG;
+  std::string fb = std::string(folder) + "/begin.bin", fa = std::string(folder) + "/adjacent.bin";
+  FILE *f = fopen(fb.c_str(), "wb");
+  if (!f) return TRUST_TC_E_IO;
+  bool ok = fwrite(beg, sizeof(int64_t), (size_t)(n + 1), f) == (size_t)(n + 1);
+  ok &= fclose(f) == 0;
+  f = fopen(fa.c_str(), "wb");
+  if (!f) return TRUST_TC_E_IO;
+  if (m) ok &= fwrite(adj, sizeof(int32_t), (size_t)m, f) == (size_t)m;
+  ok &= fclose(f) == 0;
+  return ok ? TRUST_TC_OK : TRUST_TC_E_IO;
+}
+
+int trust_tc_count_folder(const char *folder, const trust_tc_opts *opts, trust_tc_result *r) {
+  if (!folder || !r) return TRUST_TC_E_ARG;
+  int64_t *beg = nullptr, n = 0, m = 0;
+  int32_t *adj = nullptr;
+  int rc = trust_tc_load_folder(folder, &beg, &adj, &n, &m);
+  if (rc) return rc;
+  trust_tc_opts o;
+  if (opts) o = *opts; else trust_tc_opts_init(&o);
+  o.ptr_kind = TRUST_TC_HOST;
+  rc = trust_tc_count_csr(nullptr, beg, adj, n, m, &o, r);
+  free(beg);
+  free(adj);
+  return rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,38 @@
+// tc_count.h — host-visible interface of the counting kernels (internal to the library).
+#pragma once
+#include "tc_common.cuh"
+
+namespace tc {
+
+struct ListOffsets {
+  int off[TC_NUM_CLASSES];  // start of each class list inside the concatenated list buffer
+};
+
+// Arguments of the persistent counting kernel.  A = rows hashed into tables, B = rows whose arcs
+// (v,u) are walked, C = rows probed (N+(u)).  For a whole graph A = B = C; for an (i,j,k) tile
+// job of the partitioned path A = part(i,j), B = part(i,k), C = part(k,j)
+// (With-graph-partition/TC.cu:992-994).
+struct CountArgs {
+  const int64_t *begA, *begB, *begC;
+  const int32_t *adjA, *adjB, *adjC;
+  int64_t rows;
+  const int *lists;
+  ListOffsets off;
+  TcControl *ctl;
+  int *huge_tables;   // global tables for the huge class: huge_blocks regions of 2^huge_log2 ints
+  int huge_log2;
+  int huge_blocks;
+  int warp_slots;     // shared-memory ints per warp in the warp phase
+  int chunk;          // items per queue claim (per group) in the warp phase
+};
+
+int launch_check(const int64_t *beg, const int32_t *adj, int64_t rows, int64_t m, int64_t id_bound,
+                 int check_ids, TcControl *ctl, int num_sms, cudaStream_t st);
+int launch_classify(int pass, const int64_t *begA, const int64_t *begB, int64_t rows, int min_deg,
+                    int warp_max, int cta_max, TcControl *ctl, int *lists, const ListOffsets &off,
+                    int num_sms, cudaStream_t st);
+int count_kernel_occupancy(bool same, int threads, size_t smem_bytes, int *blocks_per_sm);
+int launch_count(bool same, const CountArgs &a, int blocks, int threads, size_t smem_bytes,
+                 cudaStream_t st);
+
+}  // namespace tc
