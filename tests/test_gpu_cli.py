@@ -26,7 +26,8 @@ def test_cli_line(tmp_path):
     assert folder == str(tmp_path)
     assert int(n) == z["ref_beg"].size - 1 and int(m) == z["ref_adj"].size
     assert int(tri) == int(z["nx_triangles"][0])
-    assert float(t) > 0 and abs(float(teps) - int(m) / float(t) / 1e9) < 1e-3 * max(1.0, float(teps)) + 2e-6
+    # time is printed with 6 decimals, so compare GTEPS loosely against the printed time
+    assert float(t) > 0 and abs(float(teps) - int(m) / float(t) / 1e9) <= 0.1 * float(teps) + 1e-6
 
 
 def test_cli_default_knobs_and_ranks(tmp_path):

@@ -49,12 +49,13 @@ class CountResult:
     vertices: int
     edges: int
     max_out_degree: int
+    wedges: int = 0
     class_sizes: dict = field(default_factory=dict)
 
 
 def _result(r: _lib.Result) -> CountResult:
     return CountResult(int(r.triangles), r.kernel_seconds, r.count_seconds, r.call_seconds, int(r.vertices),
-                       int(r.edges), int(r.max_out_degree),
+                       int(r.edges), int(r.max_out_degree), int(r.wedges),
                        {k: int(v) for k, v in zip(CLASS_NAMES, r.class_sizes)})
 
 

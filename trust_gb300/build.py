@@ -43,6 +43,25 @@ def _cuda_home() -> str:
     return "/usr/local/cuda"
 
 
+def _arch_guard(out_dir: str, outputs: list[str]) -> None:
+    """Outputs compiled on another machine type (this tree travels between x86 and Arm hosts) are
+    removed so they are rebuilt, never linked."""
+    import platform
+    stamp = os.path.join(out_dir, ".machine")
+    here = platform.machine()
+    prev = open(stamp).read().strip() if os.path.exists(stamp) else None
+    if prev != here:
+        for d in (out_dir,):
+            for f in os.listdir(d):
+                if f.endswith((".o", ".so")):
+                    os.remove(os.path.join(d, f))
+        for o in outputs:
+            if os.path.exists(o):
+                os.remove(o)
+        with open(stamp, "w") as f:
+            f.write(here + "\n")
+
+
 def _newer(out: str, deps: list[str]) -> bool:
     if not os.path.exists(out):
         return False
@@ -64,6 +83,7 @@ def _headers() -> list[str]:
 
 def build_library(verbose: bool = False) -> str:
     os.makedirs(OBJ, exist_ok=True)
+    _arch_guard(OBJ, [LIB, CLI])
     nvcc = shutil.which("nvcc") or os.path.join(_cuda_home(), "bin", "nvcc")
     hdrs = _headers()
     jobs = []
@@ -87,6 +107,7 @@ def build_library(verbose: bool = False) -> str:
 
 def build_oracle() -> None:
     os.makedirs(ORACLE_OBJ, exist_ok=True)
+    _arch_guard(ORACLE_OBJ, [])
     src = os.path.join(ORACLE, "tc_oracle.c")
     if not _newer(ORACLE_LIB, [src]):
         _run(["gcc", "-O2", "-std=c11", "-ffp-contract=off", "-fPIC", "-shared", "-o", ORACLE_LIB, src,
