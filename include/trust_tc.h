@@ -116,6 +116,18 @@ int trust_tc_validate_csr(const int64_t *begin, const int32_t *adj, int64_t n, i
 int trust_tc_count_csr(trust_tc_ctx *ctx, const int64_t *begin, const int32_t *adj, int64_t n,
                        int64_t m, const trust_tc_opts *opts, trust_tc_result *result);
 
+/* Count over a device-resident CSR without allocating anything.  No counterpart in the
+ * reference: it is for callers that may not allocate GPU memory while they count (memory owned
+ * by their own pool under a fixed budget, or where cudaMalloc's implicit synchronisation would
+ * stall other work).  Scratch comes from one 16 MiB array in the library's device image, held by
+ * every GPU that loads the library until exit.  Limits: n <= 4,194,240 rows and every out-degree
+ * within the CTA table (default 4096); larger inputs return TRUST_TC_E_TOO_LARGE.  opts->ptr_kind
+ * must be TRUST_TC_DEVICE; timing fields of the result stay 0.  The first call on a device looks
+ * up the array's address; make it before any stream capture.  Calls that overlap on the GPU race
+ * on the shared array and must be serialised by the caller. */
+int trust_tc_count_csr_noalloc(const int64_t *d_begin, const int32_t *d_adj, int64_t n, int64_t m,
+                               const trust_tc_opts *opts, trust_tc_result *result);
+
 /* Load `<folder>/begin.bin` and `<folder>/adjacent.bin` into malloc'd host arrays.
  * Replaces graph::graph (Without-graph-partition/graph.hpp:18-67) and fsize
  * (Without-graph-partition/comm.h:26-32): n = bytes(begin)/8 - 1, m = bytes(adj)/4, with the
