@@ -70,30 +70,83 @@ __device__ __forceinline__ int group_count_le(int incl, int k) {
   return j;
 }
 
-// Probe the wedges of up to G arcs held one per lane of a G-lane group.
-// Lane state: arc target row start `s` and length `dd` (0 for idle lanes).
-// Returns this lane's hits.  All 32 lanes call it (warp-uniform loop count).
+// Membership in the source row N+(v), held in registers of every lane of the group (rows of at
+// most G <= 8 entries; lanes past the row hold -1, which no id equals).
 template <int G>
-__device__ __forceinline__ unsigned long long group_probe(const int32_t *__restrict__ adjC,
-                                                          long long s, int dd, int glane,
-                                                          const int *tab, int log2,
-                                                          unsigned long long &wedges) {
-  int incl = group_scan_incl<G>(dd, glane);
-  int tot = __shfl_sync(TC_FULL_MASK, incl, G - 1, G);
-  if (glane == 0) wedges += (unsigned)tot;
-  long long base = s - (long long)(incl - dd);
-  int totmax = __reduce_max_sync(TC_FULL_MASK, tot);
-  unsigned long long hits = 0;
-  for (int k0 = 0; k0 < totmax; k0 += G) {
-    int k = k0 + glane;
-    int j = group_count_le<G>(incl, k);
-    long long bj = __shfl_sync(TC_FULL_MASK, base, j, G);
-    if (k < tot) {
-      int w = tc_ld_nc(adjC + bj + k);
-      hits += set_probe(tab, log2, w);
+struct RegSet {
+  int key[G];
+  __device__ __forceinline__ void load(int mine) {
+#pragma unroll
+    for (int i = 0; i < G; ++i) key[i] = __shfl_sync(TC_FULL_MASK, mine, i, G);
+  }
+  __device__ __forceinline__ int has(int w) const {
+    bool h = false;
+#pragma unroll
+    for (int i = 0; i < G; ++i) h |= key[i] == w;
+    return h;
+  }
+};
+
+// Membership in an open-addressing table (shared or global memory).
+struct HashSet {
+  const int *tab;
+  int log2;
+  __device__ __forceinline__ int has(int w) const { return set_probe(tab, log2, w); }
+};
+
+constexpr int TC_UNROLL = 2;  // independent neighbour-row loads in flight per lane
+
+// Probe every wedge of the arcs held one per lane of a G-lane group against `set`.
+// Lane state: the arc's target row start `s` (int: m < 2^31) and length `dd` (0 if idle).
+// Rows of at least G entries are walked by the whole group, G consecutive entries per step
+// (coalesced, no index search); shorter rows are flattened with a shuffle prefix scan and each
+// lane finds its row by a shuffle binary search.  All 32 lanes call it.
+template <int G, class Set>
+__device__ __forceinline__ void probe_arcs(const int32_t *__restrict__ adjC, int s, int dd, int glane,
+                                           const Set &set, unsigned long long &hits,
+                                           unsigned long long &wedges) {
+  constexpr int U = TC_UNROLL;
+  wedges += (unsigned)dd;
+  const int lane = threadIdx.x & 31;
+  const int gbase = lane & ~(G - 1);
+  const unsigned gbits = G == 32 ? 0xffffffffu : ((1u << G) - 1u);
+  unsigned mine = (__ballot_sync(TC_FULL_MASK, dd >= G) >> gbase) & gbits;
+  // long rows: one row at a time per group
+  while (__any_sync(TC_FULL_MASK, mine != 0)) {
+    const bool have = mine != 0;
+    const int j = have ? __ffs(mine) - 1 : 0;
+    mine &= mine - 1;
+    const int sj = __shfl_sync(TC_FULL_MASK, s, j, G);
+    int dj = __shfl_sync(TC_FULL_MASK, dd, j, G);
+    if (!have) dj = 0;
+    for (int k = glane; k < dj; k += G * U) {
+      int w[U];
+#pragma unroll
+      for (int r = 0; r < U; ++r) w[r] = k + r * G < dj ? tc_ld_nc(adjC + sj + k + r * G) : -1;
+#pragma unroll
+      for (int r = 0; r < U; ++r)
+        if (w[r] >= 0) hits += set.has(w[r]);
     }
   }
-  return hits;
+  // short rows: flattened over the group's lanes
+  const int sd = dd < G ? dd : 0;
+  const int incl = group_scan_incl<G>(sd, glane);
+  const int tot = __shfl_sync(TC_FULL_MASK, incl, G - 1, G);
+  const int base = s - (incl - sd);
+  const int totmax = __reduce_max_sync(TC_FULL_MASK, tot);
+  for (int k0 = 0; k0 < totmax; k0 += G * U) {
+    int w[U];
+#pragma unroll
+    for (int r = 0; r < U; ++r) {
+      const int k = k0 + r * G + glane;
+      const int j = group_count_le<G>(incl, k);
+      const int bj = __shfl_sync(TC_FULL_MASK, base, j, G);
+      w[r] = k < tot ? tc_ld_nc(adjC + bj + k) : -1;
+    }
+#pragma unroll
+    for (int r = 0; r < U; ++r)
+      if (w[r] >= 0) hits += set.has(w[r]);
+  }
 }
 
 // ------------------------------------------------------------------------------------------
@@ -196,15 +249,29 @@ struct BlockShared {
   int next_batch;
 };
 
+__device__ __forceinline__ int ceil_log2_table(int d) {
+  // smallest power of two >= 2d, at least 64 slots
+  int need = max(2 * d, 64);
+  return 32 - __clz(need - 1);
+}
+
+// Row start and length of v (int: m < 2^31 is enforced on the host).
+__device__ __forceinline__ void row_of(const int64_t *__restrict__ beg, int v, int &b, int &d) {
+  const long long lo = tc_ld_nc(beg + v), hi = tc_ld_nc(beg + v + 1);
+  b = (int)lo;
+  d = (int)(hi - lo);
+}
+
 // One vertex handled by a whole CTA.  `tab` is shared (CTA class) or global (huge class).
+// Warps claim 32-arc batches of the vertex from a shared counter.
 template <bool SAME>
-__device__ void cta_vertex(const CountArgs &p, int v, int *tab, int log2, BlockShared &bs,
-                           unsigned long long &hits, unsigned long long &wedges) {
+__device__ void cta_vertex(const CountArgs &p, int v, int *tab, BlockShared &bs, unsigned long long &hits,
+                           unsigned long long &wedges) {
   const int lane = threadIdx.x & 31;
-  const int64_t bA = tc_ld_nc(p.begA + v);
-  const int dA = (int)(tc_ld_nc(p.begA + v + 1) - bA);
-  const int64_t bB = SAME ? bA : tc_ld_nc(p.begB + v);
-  const int dB = SAME ? dA : (int)(tc_ld_nc(p.begB + v + 1) - bB);
+  int bA, dA, bB, dB;
+  row_of(p.begA, v, bA, dA);
+  if (SAME) { bB = bA; dB = dA; } else { row_of(p.begB, v, bB, dB); }
+  const int log2 = ceil_log2_table(dA);
   const int T = 1 << log2;
   for (int i = threadIdx.x; i < T; i += blockDim.x) tab[i] = -1;
   if (threadIdx.x == 0) bs.next_batch = 0;
@@ -213,107 +280,84 @@ __device__ void cta_vertex(const CountArgs &p, int v, int *tab, int log2, BlockS
   for (int i = threadIdx.x; i < dA; i += blockDim.x) ok &= set_insert(tab, log2, tc_ld_nc(p.adjA + bA + i));
   if (!ok) atomicOr(&p.ctl->status, TC_DEV_TABLE_FULL);
   __syncthreads();
+  const HashSet set{tab, log2};
   const int nbatch = (dB + 31) >> 5;
   for (;;) {
     int bt = 0;
     if (lane == 0) bt = atomicAdd(&bs.next_batch, 1);
     bt = __shfl_sync(TC_FULL_MASK, bt, 0);
     if (bt >= nbatch) break;
-    int i = (bt << 5) + lane;
-    long long s = 0;
-    int dd = 0;
-    if (i < dB) {
-      int u = tc_ld_nc(p.adjB + bB + i);
-      s = tc_ld_nc(p.begC + u);
-      dd = (int)(tc_ld_nc(p.begC + u + 1) - s);
-    }
-    hits += group_probe<32>(p.adjC, s, dd, lane, tab, log2, wedges);
+    const int i = (bt << 5) + lane;
+    int s = 0, dd = 0;
+    if (i < dB) row_of(p.begC, tc_ld_nc(p.adjB + bB + i), s, dd);
+    probe_arcs<32>(p.adjC, s, dd, lane, set, hits, wedges);
   }
   __syncthreads();
 }
 
-// One vertex per G-lane group (G = 4, 8, 16, 32), out-degrees <= G.
-template <int G, bool SAME>
-__device__ __forceinline__ void group_vertices(const CountArgs &p, int v, int *warp_tab,
-                                               unsigned long long &hits, unsigned long long &wedges) {
-  constexpr int LOG2 = (G == 4 ? 2 : G == 8 ? 3 : G == 16 ? 4 : 5) + 2;  // 4G slots per group
-  const int lane = threadIdx.x & 31;
-  const int glane = lane & (G - 1);
-  int *tab = warp_tab + (lane / G) * (4 * G);
-#pragma unroll
-  for (int i = glane; i < 4 * G; i += G) tab[i] = -1;
-  __syncwarp();
-  int64_t bA = 0, bB = 0;
-  int dA = 0, dB = 0;
-  if (v >= 0) {
-    bA = tc_ld_nc(p.begA + v);
-    dA = (int)(tc_ld_nc(p.begA + v + 1) - bA);
-    if (SAME) {
-      bB = bA;
-      dB = dA;
-    } else {
-      bB = tc_ld_nc(p.begB + v);
-      dB = (int)(tc_ld_nc(p.begB + v + 1) - bB);
-    }
-  }
-  int uA = 0;
-  if (glane < dA) {
-    uA = tc_ld_nc(p.adjA + bA + glane);
-    set_insert(tab, LOG2, uA);
-  }
-  __syncwarp();
-  long long s = 0;
-  int dd = 0;
-  if (glane < dB) {
-    int u = SAME ? uA : tc_ld_nc(p.adjB + bB + glane);
-    s = tc_ld_nc(p.begC + u);
-    dd = (int)(tc_ld_nc(p.begC + u + 1) - s);
-  }
-  hits += group_probe<G>(p.adjC, s, dd, glane, tab, LOG2, wedges);
-  __syncwarp();
-}
-
-// One vertex per warp, 32 < out-degree <= warp_max: several 32-arc rounds.
+// One vertex per warp, 32 < out-degree <= warp_max: several 32-arc rounds on a warp table.
 template <bool SAME>
-__device__ __forceinline__ void warp_vertex(const CountArgs &p, int v, int *warp_tab, int log2,
-                                            unsigned long long &hits, unsigned long long &wedges) {
+__device__ __forceinline__ void warp_vertex(const CountArgs &p, int v, int *warp_tab, unsigned long long &hits,
+                                            unsigned long long &wedges) {
   const int lane = threadIdx.x & 31;
+  int bA, dA, bB, dB;
+  row_of(p.begA, v, bA, dA);
+  if (SAME) { bB = bA; dB = dA; } else { row_of(p.begB, v, bB, dB); }
+  const int log2 = ceil_log2_table(dA);
   const int T = 1 << log2;
   for (int i = lane; i < T; i += 32) warp_tab[i] = -1;
   __syncwarp();
-  const int64_t bA = tc_ld_nc(p.begA + v);
-  const int dA = (int)(tc_ld_nc(p.begA + v + 1) - bA);
-  const int64_t bB = SAME ? bA : tc_ld_nc(p.begB + v);
-  const int dB = SAME ? dA : (int)(tc_ld_nc(p.begB + v + 1) - bB);
   bool ok = true;
   for (int i = lane; i < dA; i += 32) ok &= set_insert(warp_tab, log2, tc_ld_nc(p.adjA + bA + i));
   if (!ok) atomicOr(&p.ctl->status, TC_DEV_TABLE_FULL);
   __syncwarp();
+  const HashSet set{warp_tab, log2};
   for (int a0 = 0; a0 < dB; a0 += 32) {
-    int i = a0 + lane;
-    long long s = 0;
-    int dd = 0;
-    if (i < dB) {
-      int u = tc_ld_nc(p.adjB + bB + i);
-      s = tc_ld_nc(p.begC + u);
-      dd = (int)(tc_ld_nc(p.begC + u + 1) - s);
-    }
-    hits += group_probe<32>(p.adjC, s, dd, lane, warp_tab, log2, wedges);
+    const int i = a0 + lane;
+    int s = 0, dd = 0;
+    if (i < dB) row_of(p.begC, tc_ld_nc(p.adjB + bB + i), s, dd);
+    probe_arcs<32>(p.adjC, s, dd, lane, set, hits, wedges);
   }
   __syncwarp();
 }
 
-__device__ __forceinline__ int ceil_log2_table(int d) {
-  // smallest power of two >= 2d, at least 64 slots
-  int need = max(2 * d, 64);
-  return 32 - __clz(need - 1);
+// One vertex per G-lane group (G = 4, 8, 16, 32), out-degrees <= G.  The vertex's row bounds
+// (bA, dA) were loaded one step ahead by the caller.
+template <int G, bool SAME>
+__device__ __forceinline__ void group_vertex(const CountArgs &p, int v, int bA, int dA, int *grp_tab,
+                                             unsigned long long &hits, unsigned long long &wedges) {
+  const int glane = threadIdx.x & (G - 1);
+  int bB = bA, dB = dA;
+  if (!SAME && v >= 0) row_of(p.begB, v, bB, dB);
+  const int uA = glane < dA ? tc_ld_nc(p.adjA + bA + glane) : -1;
+  const int uB = SAME ? uA : (glane < dB ? tc_ld_nc(p.adjB + bB + glane) : -1);
+  int s = 0, dd = 0;
+  if (uB >= 0) row_of(p.begC, uB, s, dd);
+  if constexpr (G <= 8) {
+    RegSet<G> set;
+    set.load(uA);
+    probe_arcs<G>(p.adjC, s, dd, glane, set, hits, wedges);
+  } else {
+    constexpr int LOG2 = (G == 16 ? 4 : 5) + 2;  // 4G slots per group
+#pragma unroll
+    for (int i = glane; i < 4 * G; i += G) grp_tab[i] = -1;
+    __syncwarp();
+    if (uA >= 0) set_insert(grp_tab, LOG2, uA);
+    __syncwarp();
+    probe_arcs<G>(p.adjC, s, dd, glane, HashSet{grp_tab, LOG2}, hits, wedges);
+    __syncwarp();
+  }
 }
 
+// Drain one group class.  Each warp claims `chunk` steps of 32/G vertices; the next step's row
+// bounds are loaded while the current step is probed.
 template <int G, bool SAME>
-__device__ void drain_group_class(const CountArgs &p, int c, int *warp_tab,
-                                  unsigned long long &hits, unsigned long long &wedges) {
+__device__ void drain_group_class(const CountArgs &p, int c, int *warp_tab, unsigned long long &hits,
+                                  unsigned long long &wedges) {
   constexpr int GPW = 32 / G;
   const int lane = threadIdx.x & 31;
+  const int g = lane / G;
+  int *grp_tab = warp_tab + g * (4 * G);
   const int n_items = p.ctl->class_count[c];
   const int *list = p.lists + p.off.off[c];
   const int claim = p.chunk * GPW;
@@ -323,16 +367,31 @@ __device__ void drain_group_class(const CountArgs &p, int c, int *warp_tab,
     t0 = __shfl_sync(TC_FULL_MASK, t0, 0);
     if (t0 >= n_items) break;
     const int t1 = min(t0 + claim, n_items);
+    int v = t0 + g < t1 ? list[t0 + g] : -1;
+    int vn = t0 + GPW + g < t1 ? list[t0 + GPW + g] : -1;
+    int b = 0, d = 0;
+    if (v >= 0) row_of(p.begA, v, b, d);
     for (int t = t0; t < t1; t += GPW) {
-      int item = t + lane / G;
-      int v = item < t1 ? list[item] : -1;
-      group_vertices<G, SAME>(p, v, warp_tab, hits, wedges);
+      // prefetch: row bounds of the next step, list entry of the one after
+      int bn = 0, dn = 0;
+      if (vn >= 0) row_of(p.begA, vn, bn, dn);
+      const int item2 = t + 2 * GPW + g;
+      const int vnn = item2 < t1 ? list[item2] : -1;
+      group_vertex<G, SAME>(p, v, b, d, grp_tab, hits, wedges);
+      v = vn;
+      vn = vnn;
+      b = bn;
+      d = dn;
     }
   }
 }
 
-template <bool SAME>
-__global__ void __launch_bounds__(1024, 1) count_kernel(CountArgs p) {
+// Two register budgets: up to 1024 threads per CTA (reference launch shape), or <= 256 threads
+// with at least TC_MIN_CTAS_256 CTAs resident per SM (the default shape).
+constexpr int TC_MIN_CTAS_256 = 5;
+
+template <bool SAME, int MAXT, int MINB>
+__global__ void __launch_bounds__(MAXT, MINB) count_kernel(CountArgs p) {
   extern __shared__ int smem[];
   __shared__ BlockShared bs;
   const int lane = threadIdx.x & 31;
@@ -354,9 +413,7 @@ __global__ void __launch_bounds__(1024, 1) count_kernel(CountArgs p) {
       __syncthreads();
       const int t = bs.item;
       if (t >= n_items) break;
-      const int v = list[t];
-      const int dA = (int)(tc_ld_nc(p.begA + v + 1) - tc_ld_nc(p.begA + v));
-      cta_vertex<SAME>(p, v, tab, ceil_log2_table(dA), bs, hits, wedges);
+      cta_vertex<SAME>(p, list[t], tab, bs, hits, wedges);
     }
   }
   __syncthreads();
@@ -373,11 +430,7 @@ __global__ void __launch_bounds__(1024, 1) count_kernel(CountArgs p) {
       t0 = __shfl_sync(TC_FULL_MASK, t0, 0);
       if (t0 >= n_items) break;
       const int t1 = min(t0 + p.chunk, n_items);
-      for (int t = t0; t < t1; ++t) {
-        const int v = list[t];
-        const int dA = (int)(tc_ld_nc(p.begA + v + 1) - tc_ld_nc(p.begA + v));
-        warp_vertex<SAME>(p, v, warp_tab, ceil_log2_table(dA), hits, wedges);
-      }
+      for (int t = t0; t < t1; ++t) warp_vertex<SAME>(p, list[t], warp_tab, hits, wedges);
     }
   }
   drain_group_class<32, SAME>(p, TC_CLASS_G32, warp_tab, hits, wedges);
@@ -425,27 +478,41 @@ int launch_classify(int pass, const int64_t *begA, const int64_t *begB, int64_t 
   return TRUST_TC_OK;
 }
 
+template <bool SAME, int MAXT, int MINB>
+static cudaError_t occupancy_of(int threads, size_t smem_bytes, int *blocks_per_sm) {
+  cudaError_t e = cudaFuncSetAttribute(count_kernel<SAME, MAXT, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem_bytes);
+  if (e == cudaSuccess)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, count_kernel<SAME, MAXT, MINB>, threads,
+                                                      smem_bytes);
+  return e;
+}
+
 int count_kernel_occupancy(bool same, int threads, size_t smem_bytes, int *blocks_per_sm) {
   cudaError_t e;
-  if (same) {
-    e = cudaFuncSetAttribute(count_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
-    if (e == cudaSuccess)
-      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, count_kernel<true>, threads, smem_bytes);
-  } else {
-    e = cudaFuncSetAttribute(count_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
-    if (e == cudaSuccess)
-      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, count_kernel<false>, threads, smem_bytes);
-  }
+  if (threads <= 256)
+    e = same ? occupancy_of<true, 256, TC_MIN_CTAS_256>(threads, smem_bytes, blocks_per_sm)
+             : occupancy_of<false, 256, TC_MIN_CTAS_256>(threads, smem_bytes, blocks_per_sm);
+  else
+    e = same ? occupancy_of<true, 1024, 1>(threads, smem_bytes, blocks_per_sm)
+             : occupancy_of<false, 1024, 1>(threads, smem_bytes, blocks_per_sm);
   TC_CUDA_TRY(e);
   return TRUST_TC_OK;
 }
 
 int launch_count(bool same, const CountArgs &a, int blocks, int threads, size_t smem_bytes,
                  cudaStream_t st) {
-  if (same)
-    count_kernel<true><<<blocks, threads, smem_bytes, st>>>(a);
-  else
-    count_kernel<false><<<blocks, threads, smem_bytes, st>>>(a);
+  if (threads <= 256) {
+    if (same)
+      count_kernel<true, 256, TC_MIN_CTAS_256><<<blocks, threads, smem_bytes, st>>>(a);
+    else
+      count_kernel<false, 256, TC_MIN_CTAS_256><<<blocks, threads, smem_bytes, st>>>(a);
+  } else {
+    if (same)
+      count_kernel<true, 1024, 1><<<blocks, threads, smem_bytes, st>>>(a);
+    else
+      count_kernel<false, 1024, 1><<<blocks, threads, smem_bytes, st>>>(a);
+  }
   TC_CUDA_TRY(cudaGetLastError());
   return TRUST_TC_OK;
 }
