@@ -24,9 +24,13 @@ namespace tc {
 // ------------------------------------------------------------------------------------------
 // hash-set primitives (open addressing, linear probing, -1 = empty; ids are validated >= 0)
 // ------------------------------------------------------------------------------------------
+// Tables are 2^log2 int slots (log2 >= 6) read as buckets of four (16-byte loads).  A key's home
+// is the first slot of bucket hash(key); insertion takes the first free slot from there on
+// (linear probing over slots), so a lookup that finds an empty slot in a bucket without the key
+// can stop: the key would have been placed there.
 __device__ __forceinline__ bool set_insert(int *tab, int log2, int key) {
   const unsigned mask = (1u << log2) - 1u;
-  unsigned h = tc_hash((unsigned)key, log2);
+  unsigned h = tc_hash((unsigned)key, log2 - 2) << 2;
   for (unsigned it = 0; it <= mask; ++it) {
     int prev = atomicCAS(tab + h, -1, key);
     if (prev == -1 || prev == key) return true;
@@ -36,13 +40,13 @@ __device__ __forceinline__ bool set_insert(int *tab, int log2, int key) {
 }
 
 __device__ __forceinline__ int set_probe(const int *tab, int log2, int key) {
-  const unsigned mask = (1u << log2) - 1u;
-  unsigned h = tc_hash((unsigned)key, log2);
-  for (unsigned it = 0; it <= mask; ++it) {
-    int x = tab[h];
-    if (x == key) return 1;
-    if (x < 0) return 0;
-    h = (h + 1u) & mask;
+  const unsigned bmask = (1u << (log2 - 2)) - 1u;
+  unsigned b = tc_hash((unsigned)key, log2 - 2);
+  for (unsigned it = 0; it <= bmask; ++it) {
+    const int4 q = *reinterpret_cast<const int4 *>(tab + (b << 2));
+    if (q.x == key || q.y == key || q.z == key || q.w == key) return 1;
+    if ((q.x | q.y | q.z | q.w) < 0) return 0;  // an empty slot (-1) ends the search
+    b = (b + 1u) & bmask;
   }
   return 0;
 }
@@ -94,14 +98,15 @@ struct HashSet {
   __device__ __forceinline__ int has(int w) const { return set_probe(tab, log2, w); }
 };
 
-constexpr int TC_UNROLL = 2;  // independent neighbour-row loads in flight per lane
+constexpr int TC_UNROLL = 4;  // independent neighbour-row loads in flight per lane
 
 // Probe every wedge of the arcs held one per lane of a G-lane group against `set`.
 // Lane state: the arc's target row start `s` (int: m < 2^31) and length `dd` (0 if idle).
-// Rows of at least G entries are walked by the whole group, G consecutive entries per step
-// (coalesced, no index search); shorter rows are flattened with a shuffle prefix scan and each
-// lane finds its row by a shuffle binary search.  All 32 lanes call it.
-template <int G, class Set>
+// Rows of at least LONG entries are walked by the whole group, G consecutive entries per load
+// (coalesced, no index search), with the next U loads issued before the current U are probed;
+// shorter rows are flattened with a shuffle prefix scan and each lane finds its row by a shuffle
+// binary search.  All 32 lanes call it.
+template <int G, int LONG, class Set>
 __device__ __forceinline__ void probe_arcs(const int32_t *__restrict__ adjC, int s, int dd, int glane,
                                            const Set &set, unsigned long long &hits,
                                            unsigned long long &wedges) {
@@ -110,7 +115,7 @@ __device__ __forceinline__ void probe_arcs(const int32_t *__restrict__ adjC, int
   const int lane = threadIdx.x & 31;
   const int gbase = lane & ~(G - 1);
   const unsigned gbits = G == 32 ? 0xffffffffu : ((1u << G) - 1u);
-  unsigned mine = (__ballot_sync(TC_FULL_MASK, dd >= G) >> gbase) & gbits;
+  unsigned mine = (__ballot_sync(TC_FULL_MASK, dd >= LONG) >> gbase) & gbits;
   // long rows: one row at a time per group
   while (__any_sync(TC_FULL_MASK, mine != 0)) {
     const bool have = mine != 0;
@@ -119,17 +124,24 @@ __device__ __forceinline__ void probe_arcs(const int32_t *__restrict__ adjC, int
     const int sj = __shfl_sync(TC_FULL_MASK, s, j, G);
     int dj = __shfl_sync(TC_FULL_MASK, dd, j, G);
     if (!have) dj = 0;
-    for (int k = glane; k < dj; k += G * U) {
-      int w[U];
+    const int32_t *row = adjC + sj;
+    int w[U];
 #pragma unroll
-      for (int r = 0; r < U; ++r) w[r] = k + r * G < dj ? tc_ld_nc(adjC + sj + k + r * G) : -1;
+    for (int r = 0; r < U; ++r) w[r] = glane + r * G < dj ? tc_ld_nc(row + glane + r * G) : -1;
+    for (int k = glane; k < dj; k += G * U) {
+      const int kn = k + G * U;
+      int wn[U];
+#pragma unroll
+      for (int r = 0; r < U; ++r) wn[r] = kn + r * G < dj ? tc_ld_nc(row + kn + r * G) : -1;
 #pragma unroll
       for (int r = 0; r < U; ++r)
         if (w[r] >= 0) hits += set.has(w[r]);
+#pragma unroll
+      for (int r = 0; r < U; ++r) w[r] = wn[r];
     }
   }
   // short rows: flattened over the group's lanes
-  const int sd = dd < G ? dd : 0;
+  const int sd = dd < LONG ? dd : 0;
   const int incl = group_scan_incl<G>(sd, glane);
   const int tot = __shfl_sync(TC_FULL_MASK, incl, G - 1, G);
   const int base = s - (incl - sd);
@@ -148,6 +160,12 @@ __device__ __forceinline__ void probe_arcs(const int32_t *__restrict__ adjC, int
       if (w[r] >= 0) hits += set.has(w[r]);
   }
 }
+
+// Rows at least this long are walked row by row by a group of G lanes.
+template <int G>
+struct LongRow {
+  static constexpr int value = G;
+};
 
 // ------------------------------------------------------------------------------------------
 // validation / classification
@@ -290,7 +308,7 @@ __device__ void cta_vertex(const CountArgs &p, int v, int *tab, BlockShared &bs,
     const int i = (bt << 5) + lane;
     int s = 0, dd = 0;
     if (i < dB) row_of(p.begC, tc_ld_nc(p.adjB + bB + i), s, dd);
-    probe_arcs<32>(p.adjC, s, dd, lane, set, hits, wedges);
+    probe_arcs<32, LongRow<32>::value>(p.adjC, s, dd, lane, set, hits, wedges);
   }
   __syncthreads();
 }
@@ -316,27 +334,22 @@ __device__ __forceinline__ void warp_vertex(const CountArgs &p, int v, int *warp
     const int i = a0 + lane;
     int s = 0, dd = 0;
     if (i < dB) row_of(p.begC, tc_ld_nc(p.adjB + bB + i), s, dd);
-    probe_arcs<32>(p.adjC, s, dd, lane, set, hits, wedges);
+    probe_arcs<32, LongRow<32>::value>(p.adjC, s, dd, lane, set, hits, wedges);
   }
   __syncwarp();
 }
 
-// One vertex per G-lane group (G = 4, 8, 16, 32), out-degrees <= G.  The vertex's row bounds
-// (bA, dA) were loaded one step ahead by the caller.
+// One vertex per G-lane group (G = 4, 8, 16, 32), out-degrees <= G.  The group's row entry uA
+// (this lane's element of N+(v), or -1) and the arc's target row (s, dd) were loaded ahead by
+// the caller's pipeline.
 template <int G, bool SAME>
-__device__ __forceinline__ void group_vertex(const CountArgs &p, int v, int bA, int dA, int *grp_tab,
+__device__ __forceinline__ void group_vertex(const CountArgs &p, int uA, int s, int dd, int *grp_tab,
                                              unsigned long long &hits, unsigned long long &wedges) {
   const int glane = threadIdx.x & (G - 1);
-  int bB = bA, dB = dA;
-  if (!SAME && v >= 0) row_of(p.begB, v, bB, dB);
-  const int uA = glane < dA ? tc_ld_nc(p.adjA + bA + glane) : -1;
-  const int uB = SAME ? uA : (glane < dB ? tc_ld_nc(p.adjB + bB + glane) : -1);
-  int s = 0, dd = 0;
-  if (uB >= 0) row_of(p.begC, uB, s, dd);
   if constexpr (G <= 8) {
     RegSet<G> set;
     set.load(uA);
-    probe_arcs<G>(p.adjC, s, dd, glane, set, hits, wedges);
+    probe_arcs<G, LongRow<G>::value>(p.adjC, s, dd, glane, set, hits, wedges);
   } else {
     constexpr int LOG2 = (G == 16 ? 4 : 5) + 2;  // 4G slots per group
 #pragma unroll
@@ -344,44 +357,77 @@ __device__ __forceinline__ void group_vertex(const CountArgs &p, int v, int bA, 
     __syncwarp();
     if (uA >= 0) set_insert(grp_tab, LOG2, uA);
     __syncwarp();
-    probe_arcs<G>(p.adjC, s, dd, glane, HashSet{grp_tab, LOG2}, hits, wedges);
+    probe_arcs<G, LongRow<G>::value>(p.adjC, s, dd, glane, HashSet{grp_tab, LOG2}, hits, wedges);
     __syncwarp();
   }
 }
 
-// Drain one group class.  Each warp claims `chunk` steps of 32/G vertices; the next step's row
-// bounds are loaded while the current step is probed.
+// Pipeline state of one group for one vertex: the list entry, its row, this lane's row element
+// and that element's target row.
+struct GroupStage {
+  int v, b, d, uA, uB, s, dd;
+};
+
+// Drain one group class.  Each warp claims `chunk` steps of 32/G vertices.  Loads run three
+// steps ahead: while step t is probed, step t+1's target rows, step t+2's row elements and
+// step t+3's row bounds are in flight (the reference walks this chain serially per vertex).
 template <int G, bool SAME>
 __device__ void drain_group_class(const CountArgs &p, int c, int *warp_tab, unsigned long long &hits,
                                   unsigned long long &wedges) {
   constexpr int GPW = 32 / G;
   const int lane = threadIdx.x & 31;
   const int g = lane / G;
+  const int glane = lane & (G - 1);
   int *grp_tab = warp_tab + g * (4 * G);
   const int n_items = p.ctl->class_count[c];
   const int *list = p.lists + p.off.off[c];
   const int claim = p.chunk * GPW;
+  // stage loaders
+  auto ld_v = [&](int item, int t1) { return item < t1 ? list[item] : -1; };
+  auto ld_row = [&](GroupStage &x) {
+    x.b = 0; x.d = 0;
+    if (x.v >= 0) row_of(p.begA, x.v, x.b, x.d);
+  };
+  auto ld_elem = [&](GroupStage &x) {
+    x.uA = glane < x.d ? tc_ld_nc(p.adjA + x.b + glane) : -1;
+    if (SAME) {
+      x.uB = x.uA;
+    } else {
+      int bB = 0, dB = 0;
+      if (x.v >= 0) row_of(p.begB, x.v, bB, dB);
+      x.uB = glane < dB ? tc_ld_nc(p.adjB + bB + glane) : -1;
+    }
+  };
+  auto ld_target = [&](GroupStage &x) {
+    x.s = 0; x.dd = 0;
+    if (x.uB >= 0) row_of(p.begC, x.uB, x.s, x.dd);
+  };
   for (;;) {
     int t0 = 0;
     if (lane == 0) t0 = atomicAdd(&p.ctl->class_next[c], claim);
     t0 = __shfl_sync(TC_FULL_MASK, t0, 0);
     if (t0 >= n_items) break;
     const int t1 = min(t0 + claim, n_items);
-    int v = t0 + g < t1 ? list[t0 + g] : -1;
-    int vn = t0 + GPW + g < t1 ? list[t0 + GPW + g] : -1;
-    int b = 0, d = 0;
-    if (v >= 0) row_of(p.begA, v, b, d);
+    GroupStage s0, s1, s2;
+    s0.v = ld_v(t0 + g, t1);
+    s1.v = ld_v(t0 + GPW + g, t1);
+    s2.v = ld_v(t0 + 2 * GPW + g, t1);
+    ld_row(s0);
+    ld_row(s1);
+    ld_elem(s0);
+    ld_target(s0);
+    ld_elem(s1);
+    ld_row(s2);
     for (int t = t0; t < t1; t += GPW) {
-      // prefetch: row bounds of the next step, list entry of the one after
-      int bn = 0, dn = 0;
-      if (vn >= 0) row_of(p.begA, vn, bn, dn);
-      const int item2 = t + 2 * GPW + g;
-      const int vnn = item2 < t1 ? list[item2] : -1;
-      group_vertex<G, SAME>(p, v, b, d, grp_tab, hits, wedges);
-      v = vn;
-      vn = vnn;
-      b = bn;
-      d = dn;
+      GroupStage s3;
+      s3.v = ld_v(t + 3 * GPW + g, t1);
+      ld_target(s1);  // row elements of t+1 arrived during the previous step
+      ld_elem(s2);
+      ld_row(s3);
+      group_vertex<G, SAME>(p, s0.uA, s0.s, s0.dd, grp_tab, hits, wedges);
+      s0 = s1;
+      s1 = s2;
+      s2 = s3;
     }
   }
 }
