@@ -163,6 +163,22 @@ int count_device(trust_tc_ctx *c, const DevGraph3 &g, const trust_tc_opts &o, bo
     rc = ensure((void **)&c->d_huge, &c->huge_cap, per * nb);
     if (rc) return rc;
   }
+  // shared memory sized to what this graph needs: warp tables, plus a CTA table only as large as
+  // the largest CTA-class row present; the rest of the SM's unified memory stays L1
+  size_t smem = (size_t)4 * cfg.warp_slots * (cfg.threads / 32);
+  if (h.class_count[TC_CLASS_CTA] > 0) {
+    const int64_t dcta = std::min<int64_t>(h.max_out_degree, cfg.cta_max);
+    smem = std::max(smem, (size_t)4 << std::max(ceil_log2_size(2 * dcta), 6));
+  }
+  int blocks = cfg.blocks;
+  {
+    int per_sm = 0;
+    rc = count_kernel_occupancy(same, cfg.threads, smem, &per_sm);
+    if (rc) return rc;
+    if (o.blocks <= 0) blocks = c->num_sms * std::max(per_sm, 1);
+    rc = set_count_kernel_carveout(same, cfg.threads, smem, std::max(per_sm, 1));
+    if (rc) return rc;
+  }
   // 3. scatter the class lists
   rc = launch_classify(1, g.begA, g.begB, g.rows, g.min_deg, cfg.warp_max, cfg.cta_max, ctl, c->d_lists,
                        off, c->num_sms, st);
@@ -178,7 +194,7 @@ int count_device(trust_tc_ctx *c, const DevGraph3 &g, const trust_tc_opts &o, bo
   a.warp_slots = cfg.warp_slots;
   a.chunk = cfg.chunk;
   TC_CUDA_TRY(cudaEventRecord(c->ev[2], st));
-  rc = launch_count(same, a, cfg.blocks, cfg.threads, cfg.smem, st);
+  rc = launch_count(same, a, blocks, cfg.threads, smem, st);
   if (rc) return rc;
   TC_CUDA_TRY(cudaEventRecord(c->ev[3], st));
   TC_CUDA_TRY(cudaMemcpyAsync(c->h_ctl, ctl, sizeof(TcControl), cudaMemcpyDeviceToHost, st));

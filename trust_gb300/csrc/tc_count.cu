@@ -74,23 +74,6 @@ __device__ __forceinline__ int group_count_le(int incl, int k) {
   return j;
 }
 
-// Membership in the source row N+(v), held in registers of every lane of the group (rows of at
-// most G <= 8 entries; lanes past the row hold -1, which no id equals).
-template <int G>
-struct RegSet {
-  int key[G];
-  __device__ __forceinline__ void load(int mine) {
-#pragma unroll
-    for (int i = 0; i < G; ++i) key[i] = __shfl_sync(TC_FULL_MASK, mine, i, G);
-  }
-  __device__ __forceinline__ int has(int w) const {
-    bool h = false;
-#pragma unroll
-    for (int i = 0; i < G; ++i) h |= key[i] == w;
-    return h;
-  }
-};
-
 // Membership in an open-addressing table (shared or global memory).
 struct HashSet {
   const int *tab;
@@ -166,6 +149,81 @@ template <int G>
 struct LongRow {
   static constexpr int value = G;
 };
+
+// Membership of w in the source row of group g of this warp.  G <= 8: the rows are staged in
+// shared memory as G keys per group (-1 past the row), read with 16-byte loads.  G >= 16: each
+// group owns a 4G-slot hash table.
+template <int G>
+__device__ __forceinline__ int group_has(const int *wtab, int g, int w) {
+  if constexpr (G == 4) {
+    const int4 q = *reinterpret_cast<const int4 *>(wtab + 4 * g);
+    return (q.x == w) | (q.y == w) | (q.z == w) | (q.w == w);
+  } else if constexpr (G == 8) {
+    const int4 q0 = *reinterpret_cast<const int4 *>(wtab + 8 * g);
+    const int4 q1 = *reinterpret_cast<const int4 *>(wtab + 8 * g + 4);
+    return (q0.x == w) | (q0.y == w) | (q0.z == w) | (q0.w == w) | (q1.x == w) | (q1.y == w) | (q1.z == w) |
+           (q1.w == w);
+  } else {
+    constexpr int LOG2 = (G == 16 ? 4 : 5) + 2;
+    return set_probe(wtab + g * (4 * G), LOG2, w);
+  }
+}
+
+// Probe every wedge of a warp whose lanes hold one arc each, lanes [gG, gG+G) belonging to
+// vertex g.  Unlike probe_arcs, the wedges of all groups are flattened into one list over the
+// 32 lanes, so a round costs the same whatever the spread of work between groups; a wedge finds
+// its arc by a shuffle binary search and its group's set by the arc's lane.  Rows of at least
+// 32 * TC_UNROLL entries are walked by the whole warp instead (keeps wedge indices small).
+template <int G>
+__device__ __forceinline__ void probe_warp_flat(const int32_t *__restrict__ adjC, int s, int dd,
+                                                const int *wtab, unsigned long long &hits,
+                                                unsigned long long &wedges) {
+  constexpr int U = TC_UNROLL;
+  constexpr int LONG = 32 * U;
+  const int lane = threadIdx.x & 31;
+  wedges += (unsigned)dd;
+  unsigned lm = __ballot_sync(TC_FULL_MASK, dd >= LONG);
+  while (lm) {
+    const int j = __ffs(lm) - 1;
+    lm &= lm - 1;
+    const int sj = __shfl_sync(TC_FULL_MASK, s, j);
+    const int dj = __shfl_sync(TC_FULL_MASK, dd, j);
+    const int g = j / G;
+    const int32_t *row = adjC + sj;
+    int w[U];
+#pragma unroll
+    for (int r = 0; r < U; ++r) w[r] = lane + r * 32 < dj ? tc_ld_nc(row + lane + r * 32) : -1;
+    for (int k = lane; k < dj; k += 32 * U) {
+      const int kn = k + 32 * U;
+      int wn[U];
+#pragma unroll
+      for (int r = 0; r < U; ++r) wn[r] = kn + r * 32 < dj ? tc_ld_nc(row + kn + r * 32) : -1;
+#pragma unroll
+      for (int r = 0; r < U; ++r)
+        if (w[r] >= 0) hits += group_has<G>(wtab, g, w[r]);
+#pragma unroll
+      for (int r = 0; r < U; ++r) w[r] = wn[r];
+    }
+  }
+  const int sd = dd < LONG ? dd : 0;
+  const int incl = group_scan_incl<32>(sd, lane);
+  const int tot = __shfl_sync(TC_FULL_MASK, incl, 31);
+  const int base = s - (incl - sd);
+  for (int k0 = 0; k0 < tot; k0 += 32 * U) {
+    int w[U], g[U];
+#pragma unroll
+    for (int r = 0; r < U; ++r) {
+      const int k = k0 + r * 32 + lane;
+      const int j = group_count_le<32>(incl, k);
+      const int bj = __shfl_sync(TC_FULL_MASK, base, j);
+      g[r] = j / G;
+      w[r] = k < tot ? tc_ld_nc(adjC + bj + k) : -1;
+    }
+#pragma unroll
+    for (int r = 0; r < U; ++r)
+      if (w[r] >= 0) hits += group_has<G>(wtab, g[r], w[r]);
+  }
+}
 
 // ------------------------------------------------------------------------------------------
 // validation / classification
@@ -343,23 +401,24 @@ __device__ __forceinline__ void warp_vertex(const CountArgs &p, int v, int *warp
 // (this lane's element of N+(v), or -1) and the arc's target row (s, dd) were loaded ahead by
 // the caller's pipeline.
 template <int G, bool SAME>
-__device__ __forceinline__ void group_vertex(const CountArgs &p, int uA, int s, int dd, int *grp_tab,
+__device__ __forceinline__ void group_vertex(const CountArgs &p, int uA, int s, int dd, int *wtab,
                                              unsigned long long &hits, unsigned long long &wedges) {
-  const int glane = threadIdx.x & (G - 1);
+  const int lane = threadIdx.x & 31;
+  const int g = lane / G;
+  const int glane = lane & (G - 1);
   if constexpr (G <= 8) {
-    RegSet<G> set;
-    set.load(uA);
-    probe_arcs<G, LongRow<G>::value>(p.adjC, s, dd, glane, set, hits, wedges);
+    wtab[lane] = uA;  // group g's keys at wtab[gG .. gG+G)
   } else {
     constexpr int LOG2 = (G == 16 ? 4 : 5) + 2;  // 4G slots per group
+    int *tab = wtab + g * (4 * G);
 #pragma unroll
-    for (int i = glane; i < 4 * G; i += G) grp_tab[i] = -1;
+    for (int i = glane; i < 4 * G; i += G) tab[i] = -1;
     __syncwarp();
-    if (uA >= 0) set_insert(grp_tab, LOG2, uA);
-    __syncwarp();
-    probe_arcs<G, LongRow<G>::value>(p.adjC, s, dd, glane, HashSet{grp_tab, LOG2}, hits, wedges);
-    __syncwarp();
+    if (uA >= 0) set_insert(tab, LOG2, uA);
   }
+  __syncwarp();
+  probe_warp_flat<G>(p.adjC, s, dd, wtab, hits, wedges);
+  __syncwarp();
 }
 
 // Pipeline state of one group for one vertex: the list entry, its row, this lane's row element
@@ -378,7 +437,6 @@ __device__ void drain_group_class(const CountArgs &p, int c, int *warp_tab, unsi
   const int lane = threadIdx.x & 31;
   const int g = lane / G;
   const int glane = lane & (G - 1);
-  int *grp_tab = warp_tab + g * (4 * G);
   const int n_items = p.ctl->class_count[c];
   const int *list = p.lists + p.off.off[c];
   const int claim = p.chunk * GPW;
@@ -424,7 +482,7 @@ __device__ void drain_group_class(const CountArgs &p, int c, int *warp_tab, unsi
       ld_target(s1);  // row elements of t+1 arrived during the previous step
       ld_elem(s2);
       ld_row(s3);
-      group_vertex<G, SAME>(p, s0.uA, s0.s, s0.dd, grp_tab, hits, wedges);
+      group_vertex<G, SAME>(p, s0.uA, s0.s, s0.dd, warp_tab, hits, wedges);
       s0 = s1;
       s1 = s2;
       s2 = s3;
@@ -542,6 +600,25 @@ int count_kernel_occupancy(bool same, int threads, size_t smem_bytes, int *block
   else
     e = same ? occupancy_of<true, 1024, 1>(threads, smem_bytes, blocks_per_sm)
              : occupancy_of<false, 1024, 1>(threads, smem_bytes, blocks_per_sm);
+  TC_CUDA_TRY(e);
+  return TRUST_TC_OK;
+}
+
+template <bool SAME, int MAXT, int MINB>
+static cudaError_t carveout_of(int pct) {
+  return cudaFuncSetAttribute(count_kernel<SAME, MAXT, MINB>, cudaFuncAttributePreferredSharedMemoryCarveout, pct);
+}
+
+int set_count_kernel_carveout(bool same, int threads, size_t smem_bytes, int per_sm) {
+  // per-CTA reservation of 1 KiB on top of the dynamic and static shared memory
+  const double need = (double)per_sm * (double)(smem_bytes + 2048);
+  int pct = (int)(100.0 * need / (228.0 * 1024.0)) + 1;
+  pct = std::min(std::max(pct, 0), 100);
+  cudaError_t e;
+  if (threads <= 256)
+    e = same ? carveout_of<true, 256, TC_MIN_CTAS_256>(pct) : carveout_of<false, 256, TC_MIN_CTAS_256>(pct);
+  else
+    e = same ? carveout_of<true, 1024, 1>(pct) : carveout_of<false, 1024, 1>(pct);
   TC_CUDA_TRY(e);
   return TRUST_TC_OK;
 }

@@ -32,6 +32,8 @@ int launch_classify(int pass, const int64_t *begA, const int64_t *begB, int64_t 
                     int warp_max, int cta_max, TcControl *ctl, int *lists, const ListOffsets &off,
                     int num_sms, cudaStream_t st);
 int count_kernel_occupancy(bool same, int threads, size_t smem_bytes, int *blocks_per_sm);
+// Shared-memory carveout hint: just enough for `per_sm` resident CTAs of `smem_bytes` each.
+int set_count_kernel_carveout(bool same, int threads, size_t smem_bytes, int per_sm);
 int launch_count(bool same, const CountArgs &a, int blocks, int threads, size_t smem_bytes,
                  cudaStream_t st);
 
