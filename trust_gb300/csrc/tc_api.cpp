@@ -102,7 +102,7 @@ static int resolve_cfg(trust_tc_ctx *c, const trust_tc_opts &o, bool same, Launc
   cfg->smem = std::max(table_bytes, warp_bytes);
   if (cfg->smem > (size_t)c->max_smem_optin) return TRUST_TC_E_ARG;
   cfg->cta_max = 1 << (cfg->cta_log2 - 1);
-  cfg->chunk = o.chunk > 0 ? o.chunk : 4;
+  cfg->chunk = o.chunk > 0 ? o.chunk : 8;
   int per_sm = 0;
   int st = count_kernel_occupancy(same, cfg->threads, cfg->smem, &per_sm);
   if (st) return st;

@@ -150,6 +150,21 @@ struct LongRow {
   static constexpr int value = G;
 };
 
+// Position (0..31) of the n-th (0-based) set bit of mask; mask must have more than n set bits.
+__device__ __forceinline__ int nth_set_bit(unsigned mask, int n) {
+  int pos = 0;
+#pragma unroll
+  for (int step = 16; step >= 1; step >>= 1) {
+    const int cnt = __popc(mask & ((1u << step) - 1u));
+    if (n >= cnt) {
+      n -= cnt;
+      mask >>= step;
+      pos += step;
+    }
+  }
+  return pos;
+}
+
 // Membership of w in the source row of group g of this warp.  G <= 8: the rows are staged in
 // shared memory as G keys per group (-1 past the row), read with 16-byte loads.  G >= 16: each
 // group owns a 4G-slot hash table.
@@ -205,18 +220,36 @@ __device__ __forceinline__ void probe_warp_flat(const int32_t *__restrict__ adjC
       for (int r = 0; r < U; ++r) w[r] = wn[r];
     }
   }
+  // Short rows: flatten.  The nonempty arcs are ranked once (rank c is held by lane c after a
+  // gather); a round of 32 consecutive wedges then finds each wedge's arc from the bit mask of
+  // arcs starting inside the round: owner rank = arcs started before the round + starts at or
+  // before this lane's position - 1.
   const int sd = dd < LONG ? dd : 0;
   const int incl = group_scan_incl<32>(sd, lane);
   const int tot = __shfl_sync(TC_FULL_MASK, incl, 31);
-  const int base = s - (incl - sd);
+  if (tot == 0) return;
+  const unsigned ne = __ballot_sync(TC_FULL_MASK, sd > 0);
+  const int nc = __popc(ne);
+  const int src = lane < nc ? nth_set_bit(ne, lane) : 0;
+  const int src_excl = __shfl_sync(TC_FULL_MASK, incl - sd, src);  // all lanes shuffle, then select
+  const int cexcl = lane < nc ? src_excl : 0x7fffffff;
+  const int cbase = __shfl_sync(TC_FULL_MASK, s - (incl - sd), src);
+  const int cgrp = src / G;
+  int before = 0;  // ranked arcs that start before the current round
+  const unsigned upto = 0xffffffffu >> (31 - lane);
   for (int k0 = 0; k0 < tot; k0 += 32 * U) {
     int w[U], g[U];
 #pragma unroll
     for (int r = 0; r < U; ++r) {
-      const int k = k0 + r * 32 + lane;
-      const int j = group_count_le<32>(incl, k);
-      const int bj = __shfl_sync(TC_FULL_MASK, base, j);
-      g[r] = j / G;
+      const int kr = k0 + 32 * r;
+      const unsigned starts =
+          __reduce_or_sync(TC_FULL_MASK, (cexcl >= kr && cexcl < kr + 32) ? (1u << (cexcl - kr)) : 0u);
+      const int c = before + __popc(starts & upto) - 1;
+      before += __popc(starts);
+      const int cc = c < 0 ? 0 : c;
+      const int bj = __shfl_sync(TC_FULL_MASK, cbase, cc);
+      g[r] = __shfl_sync(TC_FULL_MASK, cgrp, cc);
+      const int k = kr + lane;
       w[r] = k < tot ? tc_ld_nc(adjC + bj + k) : -1;
     }
 #pragma unroll
@@ -530,10 +563,12 @@ __global__ void __launch_bounds__(MAXT, MINB) count_kernel(CountArgs p) {
     const int *list = p.lists + p.off.off[c];
     for (;;) {
       int t0 = 0;
-      if (lane == 0) t0 = atomicAdd(&p.ctl->class_next[c], p.chunk);
+      // warp-class vertices are large: claim them one at a time unless the chunk is very coarse
+      const int claim = max(1, p.chunk / 8);
+      if (lane == 0) t0 = atomicAdd(&p.ctl->class_next[c], claim);
       t0 = __shfl_sync(TC_FULL_MASK, t0, 0);
       if (t0 >= n_items) break;
-      const int t1 = min(t0 + p.chunk, n_items);
+      const int t1 = min(t0 + claim, n_items);
       for (int t = t0; t < t1; ++t) warp_vertex<SAME>(p, list[t], warp_tab, hits, wedges);
     }
   }

@@ -126,7 +126,7 @@ extern "C" int trust_tc_count_csr_noalloc(const int64_t *d_begin, const int32_t 
   a.off = off;
   a.ctl = ctl;
   a.warp_slots = warp_slots;
-  a.chunk = o.chunk > 0 ? o.chunk : 4;
+  a.chunk = o.chunk > 0 ? o.chunk : 8;
   rc = tc::launch_count(true, a, blocks, threads, smem, st);
   if (rc) return rc;
   TcControl done;
