@@ -49,8 +49,11 @@ enum { TRUST_TC_HOST = 0, TRUST_TC_DEVICE = 1 };
 
 /* work schedule; only the schedule changes, never the integer arithmetic */
 enum {
-  TRUST_TC_SCHED_PLAIN = 0,   /* degree-threshold classes (the reference's USE_CTA/USE_WARP split)  */
-  TRUST_TC_SCHED_LEARNED = 1  /* per-vertex cost model decides class and queue order                */
+  TRUST_TC_SCHED_PLAIN = 0,   /* the reference's split: one warp per vertex for out-degree 2..100,
+                                 one CTA above (USE_WARP / USE_CTA, Without-graph-partition/TC.cu:19-20) */
+  TRUST_TC_SCHED_LEARNED = 1, /* TUNED classes, then a per-vertex cost model promotes heavy vertices
+                                 to CTA granularity and orders the CTA and warp queues by cost       */
+  TRUST_TC_SCHED_TUNED = 2    /* sub-warp degree classes (4, 8, 16, 32 lanes), warp, CTA (default)   */
 };
 
 /* validation level for device-resident input (host input is always fully validated) */
@@ -69,6 +72,9 @@ typedef struct trust_tc_opts {
   int record_cycles;     /* 1: write per-vertex clock64 cycles into result->vertex_cycles       */
   void *stream;          /* cudaStream_t; NULL = legacy default stream                          */
   const float *model;    /* learned schedule: packed MLP weights (trust_tc_model_size floats)   */
+  int direction_split;   /* charge arcs with d(u) > d(v) to u's side (hash N+(u), stream N+(v)):
+                            -1 = the learned schedule decides, 0 = never, 1 = always; applied only
+                            when every row is strictly increasing (duplicate-free)             */
 } trust_tc_opts;
 
 typedef struct trust_tc_result {
@@ -188,6 +194,30 @@ double trust_tc_chung_lu_table(int64_t n, double gamma, double w_max, int64_t ta
 /* Erdos-Renyi G(n, npairs): uniform endpoint pairs. */
 int trust_tc_gen_er_device(trust_tc_ctx *ctx, int64_t n, int64_t npairs, uint64_t seed,
                            int32_t *d_pairs);
+
+/* ---- the learned schedule's per-vertex cost model ----------------------------------------
+ * An MLP, 8 fp32 features -> 32 -> 32 -> 1 (ReLU), predicting log2 of a vertex's counting cycles.
+ * Features of a vertex v with out-degree d(v) >= 2 (trust_tc_vertex_features):
+ *   log2(1+d(v)), log2(1+W), log2(1+Wmin), log2(1+max d(u)), log2(1+#arcs with d(u) > d(v)),
+ *   log2(1+W/d(v)), schedule class (0..7), log2(table slots)
+ * where W = sum over arcs (v,u) of d(u) and Wmin = sum of min(d(u), d(v)).  Trained on the GPU by
+ * this library's forward/backward/Adam kernels on cycles recorded with opts.record_cycles.
+ * No counterpart in the reference (its schedule is the fixed USE_CTA/USE_WARP split). */
+int trust_tc_model_floats(void);
+int trust_tc_model_init(float *model, uint64_t seed);
+/* mean-squared-error gradient at `model` over device arrays x (n x 8) and y (n) -> host grad */
+int trust_tc_model_grad(const float *d_x, const float *d_y, int64_t n, const float *model, float *grad,
+                        float *loss);
+/* normalise from the data, then `epochs` passes of mini-batch Adam; model is host in/out */
+int trust_tc_model_train(const float *d_x, const float *d_y, int64_t n, int epochs, int batch, float lr,
+                         float *model, float *loss);
+int trust_tc_model_predict(const float *d_x, int64_t n, const float *model, float *d_out);
+/* the model compiled into the library (trained on the generated training graphs) */
+int trust_tc_model_default(float *model);
+/* per-vertex features of a device CSR: d_features n x 8 (zeros for out-degree < 2); the schedule
+ * class is the tuned schedule's */
+int trust_tc_vertex_features(trust_tc_ctx *ctx, const int64_t *d_begin, const int32_t *d_adj, int64_t n,
+                             int64_t m, float *d_features);
 
 #ifdef __cplusplus
 }

@@ -178,3 +178,62 @@ def test_relabelled_input(ctx):
     nb[1:] = np.cumsum([len(r) for r in new_rows])
     na = np.concatenate(new_rows).astype(np.int32)
     assert T.count_csr(nb, na, ctx=ctx).triangles == int(z["nx_triangles"][0])
+
+
+@pytest.mark.parametrize("schedule", [T.SCHED_PLAIN, T.SCHED_TUNED])
+@pytest.mark.parametrize("name", ["k150", "rmat_s12", "chung_lu_3000", "er_200"])
+def test_schedules_agree(ctx, name, schedule):
+    """The schedule changes only which lanes do the work, never the count."""
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", name + ".npz"))
+    db, da = _dev(z["ref_beg"], z["ref_adj"])
+    r = T.count_csr(db, da, ctx=ctx, schedule=schedule)
+    assert r.triangles == int(z["nx_triangles"][0])
+    d = np.diff(z["ref_beg"])
+    if schedule == T.SCHED_PLAIN:  # the reference's split: warp for 2..100, CTA above
+        assert r.class_sizes["g4"] == r.class_sizes["g8"] == r.class_sizes["g16"] == r.class_sizes["g32"] == 0
+        assert r.class_sizes["warp"] == int(np.sum((d >= 2) & (d <= 100)))
+        assert r.class_sizes["cta"] + r.class_sizes["huge"] == int(np.sum(d > 100))
+
+
+def test_cycle_recording(ctx):
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "rmat_s12.npz"))
+    db, da = _dev(z["ref_beg"], z["ref_adj"])
+    n = db.numel() - 1
+    for schedule in (T.SCHED_PLAIN, T.SCHED_TUNED):
+        cyc = torch.full((n,), -1, dtype=torch.int64, device="cuda")
+        r = T.count_csr(db, da, ctx=ctx, cycles=cyc, schedule=schedule, warp_max=64, block_max=256)
+        assert r.triangles == int(z["nx_triangles"][0])
+        c = cyc.cpu().numpy()
+        d = np.diff(z["ref_beg"])
+        assert np.all(c[d < 2] == 0)
+        assert np.all(c[d >= 2] > 0)
+
+
+@pytest.mark.parametrize("name", ["k150", "rmat_s12", "chung_lu_3000", "er_200", "k60", "rmat_s9"])
+def test_direction_split(ctx, name):
+    """Charging arcs with d(u) > d(v) to u's side changes which row is hashed, not the count."""
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", name + ".npz"))
+    expect = int(z["nx_triangles"][0])
+    beg, adj = O.build_csr(z["pairs"], int(z["pairs"].max()) + 1)  # sorted, duplicate-free rows
+    db, da = _dev(beg, adj)
+    for schedule in (T.SCHED_TUNED, T.SCHED_PLAIN, T.SCHED_LEARNED):
+        r = T.count_csr(db, da, ctx=ctx, schedule=schedule, direction_split=1)
+        assert r.triangles == expect
+        d = np.diff(beg)
+        src = np.repeat(np.arange(d.size), d)
+        sel = d[src] >= 2
+        assert r.wedges == int(np.minimum(d[adj], d[src])[sel].sum())  # probes of the split plan
+    # unsorted rows (the reference preprocess output): the split is not applied, count unchanged
+    r = T.count_csr(*_dev(z["ref_beg"], z["ref_adj"]), ctx=ctx, direction_split=1)
+    assert r.triangles == expect
+    assert r.wedges == O.wedges(z["ref_beg"], z["ref_adj"])
+
+
+def test_learned_schedule_on_rmat(ctx):
+    pairs = T.gen_rmat(16, 16, seed=1)
+    beg, adj = T.build_csr(pairs, 1 << 16)
+    b, a = beg.cpu().numpy(), adj.cpu().numpy()
+    expect = O.count_forward(b, a, threads=8)
+    for schedule in (T.SCHED_LEARNED, T.SCHED_TUNED, T.SCHED_PLAIN):
+        for split in (-1, 0, 1):
+            assert T.count_csr(beg, adj, ctx=ctx, schedule=schedule, direction_split=split).triangles == expect

@@ -21,13 +21,14 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import _lib
-from ._lib import (CLASS_NAMES, DEVICE, HOST, SCHED_LEARNED, SCHED_PLAIN, VALIDATE_FULL, VALIDATE_NONE,
+from ._lib import (CLASS_NAMES, DEVICE, HOST, SCHED_LEARNED, SCHED_PLAIN, SCHED_TUNED, VALIDATE_FULL, VALIDATE_NONE,
                    VALIDATE_OFFSETS, TrustTcError, check, load)
 
 __all__ = [
     "arguments", "Triangle_count", "Context", "CountResult", "count_csr", "count_folder", "count_partitioned",
     "load_folder", "save_folder", "partition_folder", "gen_rmat", "gen_chung_lu", "gen_er", "build_csr",
-    "chung_lu_table", "TrustTcError", "load",
+    "chung_lu_table", "TrustTcError", "load", "model_floats", "model_init", "model_default", "model_grad",
+    "model_train", "model_predict", "vertex_features",
 ]
 
 
@@ -60,7 +61,7 @@ def _result(r: _lib.Result) -> CountResult:
 
 
 def _opts(threads=0, blocks=0, chunk=0, ptr_kind=HOST, validate=VALIDATE_FULL, warp_max=0, block_max=0,
-          stream=None, device=-1, schedule=SCHED_PLAIN) -> _lib.Opts:
+          stream=None, device=-1, schedule=SCHED_TUNED) -> _lib.Opts:
     o = _lib.Opts()
     load().trust_tc_opts_init(C.byref(o))
     o.device = device
@@ -107,7 +108,8 @@ def _is_torch_cuda(x) -> bool:
 
 
 def count_csr(beg, adj, *, ctx: Context | None = None, threads=0, blocks=0, chunk=0, stream=None,
-              validate=VALIDATE_FULL, warp_max=0, block_max=0) -> CountResult:
+              validate=VALIDATE_FULL, warp_max=0, block_max=0, schedule=SCHED_TUNED,
+              cycles=None, direction_split=-1, model=None) -> CountResult:
     """Count over a CSR held in numpy arrays (host) or contiguous torch CUDA tensors (device).
 
     `stream` is a cudaStream_t value (e.g. torch.cuda.current_stream().cuda_stream)."""
@@ -124,8 +126,16 @@ def count_csr(beg, adj, *, ctx: Context | None = None, threads=0, blocks=0, chun
         n, m = b.size - 1, a.size
         pb, pa, kind = b.ctypes.data_as(C.c_void_p), a.ctypes.data_as(C.c_void_p), HOST
         keep = (b, a)
-    o = _opts(threads, blocks, chunk, kind, validate, warp_max, block_max, stream)
+    o = _opts(threads, blocks, chunk, kind, validate, warp_max, block_max, stream, schedule=schedule)
+    o.direction_split = direction_split
+    if model is not None:  # host float32 array of model_floats() entries (learned schedule)
+        model = np.ascontiguousarray(model, dtype=np.float32)
+        o.model = model.ctypes.data_as(C.c_void_p)
     r = _lib.Result()
+    if cycles is not None:  # torch CUDA int64 tensor of n entries: per-vertex clock64 cycles
+        assert cycles.is_cuda and cycles.numel() >= n
+        o.record_cycles = 1
+        r.vertex_cycles = C.c_void_p(cycles.data_ptr())
     st = lib.trust_tc_count_csr(ctx.handle if ctx else None, pb, pa, n, m, C.byref(o), C.byref(r))
     del keep
     check(st, "trust_tc_count_csr")
@@ -248,3 +258,60 @@ def build_csr(pairs, id_bound: int):
         lib.trust_tc_free_device(pb)
         lib.trust_tc_free_device(pa)
     return beg, adj[: m.value]
+
+
+# ---- the learned schedule's cost model ------------------------------------------------------------
+
+def model_floats() -> int:
+    return int(load().trust_tc_model_floats())
+
+
+def model_init(seed: int = 1) -> np.ndarray:
+    m = np.zeros(model_floats(), dtype=np.float32)
+    check(load().trust_tc_model_init(m.ctypes.data_as(C.c_void_p), seed), "trust_tc_model_init")
+    return m
+
+
+def model_default():
+    """The model compiled into the library, or None before the first training run."""
+    m = np.zeros(model_floats(), dtype=np.float32)
+    st = load().trust_tc_model_default(m.ctypes.data_as(C.c_void_p))
+    return m if st == _lib.OK else None
+
+
+def model_grad(x, y, model):
+    """MSE gradient at `model` over torch CUDA float32 tensors x (N x 8) and y (N)."""
+    g = np.zeros(model_floats(), dtype=np.float32)
+    loss = C.c_float()
+    m = np.ascontiguousarray(model, dtype=np.float32)
+    check(load().trust_tc_model_grad(C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr()), x.shape[0],
+                                     m.ctypes.data_as(C.c_void_p), g.ctypes.data_as(C.c_void_p), C.byref(loss)),
+          "trust_tc_model_grad")
+    return g, float(loss.value)
+
+
+def model_train(x, y, model, epochs=100, batch=4096, lr=1e-3):
+    m = np.ascontiguousarray(model, dtype=np.float32).copy()
+    loss = C.c_float()
+    check(load().trust_tc_model_train(C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr()), x.shape[0], epochs, batch,
+                                      lr, m.ctypes.data_as(C.c_void_p), C.byref(loss)), "trust_tc_model_train")
+    return m, float(loss.value)
+
+
+def model_predict(x, model):
+    import torch
+    out = torch.empty(x.shape[0], dtype=torch.float32, device="cuda")
+    m = np.ascontiguousarray(model, dtype=np.float32)
+    check(load().trust_tc_model_predict(C.c_void_p(x.data_ptr()), x.shape[0], m.ctypes.data_as(C.c_void_p),
+                                        C.c_void_p(out.data_ptr())), "trust_tc_model_predict")
+    return out
+
+
+def vertex_features(beg, adj, ctx: Context):
+    """n x 8 float32 CUDA tensor of per-vertex features (zeros for out-degree < 2)."""
+    import torch
+    n = beg.numel() - 1
+    f = torch.empty((max(n, 1), 8), dtype=torch.float32, device="cuda")
+    check(load().trust_tc_vertex_features(ctx.handle, C.c_void_p(beg.data_ptr()), C.c_void_p(adj.data_ptr()), n,
+                                          adj.numel(), C.c_void_p(f.data_ptr())), "trust_tc_vertex_features")
+    return f[:n]

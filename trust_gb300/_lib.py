@@ -13,7 +13,7 @@ LIB_PATH = os.path.join(_HERE, "libtrust_tc.so")
 OK = 0
 E_ARG, E_IO, E_FORMAT, E_OFFSETS, E_IDS, E_TOO_LARGE, E_CUDA, E_NOMEM, E_DEVICE, E_UNSUPPORTED, E_NO_DEVICE = range(1, 12)
 HOST, DEVICE = 0, 1
-SCHED_PLAIN, SCHED_LEARNED = 0, 1
+SCHED_PLAIN, SCHED_LEARNED, SCHED_TUNED = 0, 1, 2
 VALIDATE_NONE, VALIDATE_OFFSETS, VALIDATE_FULL = 0, 1, 2
 CLASS_NAMES = ("skip", "g4", "g8", "g16", "g32", "warp", "cta", "huge")
 
@@ -32,6 +32,7 @@ class Opts(C.Structure):
         ("record_cycles", C.c_int),
         ("stream", C.c_void_p),
         ("model", C.c_void_p),
+        ("direction_split", C.c_int),
     ]
 
 
@@ -82,6 +83,13 @@ SIGNATURES = {
                                                C.c_uint64, _P]),
     "trust_tc_chung_lu_table": (C.c_double, [C.c_int64, C.c_double, C.c_double, C.c_int64, _P]),
     "trust_tc_gen_er_device": (C.c_int, [_P, C.c_int64, C.c_int64, C.c_uint64, _P]),
+    "trust_tc_model_floats": (C.c_int, []),
+    "trust_tc_model_init": (C.c_int, [_P, C.c_uint64]),
+    "trust_tc_model_grad": (C.c_int, [_P, _P, C.c_int64, _P, _P, C.POINTER(C.c_float)]),
+    "trust_tc_model_train": (C.c_int, [_P, _P, C.c_int64, C.c_int, C.c_int, C.c_float, _P, C.POINTER(C.c_float)]),
+    "trust_tc_model_predict": (C.c_int, [_P, C.c_int64, _P, _P]),
+    "trust_tc_model_default": (C.c_int, [_P]),
+    "trust_tc_vertex_features": (C.c_int, [_P, _P, _P, C.c_int64, C.c_int64, _P]),
 }
 
 _lib = None

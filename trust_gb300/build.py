@@ -33,7 +33,7 @@ ORACLE_CUDA_LIB = os.path.join(ORACLE_OBJ, "liboracle_cuda.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off", "-I" + INCLUDE]
-SOURCES = ["tc_count.cu", "tc_prep.cu", "tc_gen.cu", "tc_api.cpp", "tc_tiles.cpp", "tc_shim.cpp", "tc_noalloc.cu"]
+SOURCES = ["tc_count.cu", "tc_prep.cu", "tc_gen.cu", "tc_api.cpp", "tc_tiles.cpp", "tc_shim.cpp", "tc_noalloc.cu", "tc_split.cu", "tc_model.cu"]
 
 
 def _cuda_home() -> str:
@@ -76,7 +76,7 @@ def _run(cmd: list[str]) -> None:
 
 
 def _headers() -> list[str]:
-    hs = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
+    hs = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh", ".inc"))]
     hs += [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE)]
     return hs
 

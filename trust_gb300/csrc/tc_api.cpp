@@ -18,6 +18,7 @@
 
 #include "tc_count.h"
 #include "tc_internal.h"
+#include "tc_model.h"
 
 namespace tc {
 
@@ -44,9 +45,11 @@ int ctx_init(trust_tc_ctx *c, int device) {
   c->device = device;
   TC_CUDA_TRY(cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device));
   TC_CUDA_TRY(cudaDeviceGetAttribute(&c->max_smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device));
+  TC_CUDA_TRY(cudaDeviceGetAttribute(&c->clock_khz, cudaDevAttrClockRate, device));
   TC_CUDA_TRY(cudaMalloc(&c->d_ctl, sizeof(TcControl)));
   TC_CUDA_TRY(cudaMallocHost(&c->h_ctl, sizeof(TcControl)));
   for (auto &ev : c->ev) TC_CUDA_TRY(cudaEventCreate(&ev));
+  for (auto &ev : c->ev_split) TC_CUDA_TRY(cudaEventCreate(&ev));
   return TRUST_TC_OK;
 }
 
@@ -56,9 +59,24 @@ void ctx_release(trust_tc_ctx *c) {
   cudaFreeHost(c->h_ctl);
   cudaFree(c->d_lists);
   cudaFree(c->d_huge);
+  cudaFree(c->d_long);
+  cudaFree(c->d_split_cnt);
+  cudaFree(c->d_dec);
+  cudaFree(c->d_pred);
+  cudaFree(c->d_model);
+  cudaFree(c->d_sort);
+  cudaFree(c->d_split_wsum);
+  cudaFree(c->d_split_plans);
+  cudaFree(c->d_split_beg);
+  cudaFree(c->d_split_cbase);
+  cudaFree(c->d_split_cbeg);
+  cudaFree(c->d_split_rowmap);
+  cudaFree(c->d_split_adj);
   cudaFree(c->d_beg);
   cudaFree(c->d_adj);
   for (auto &ev : c->ev)
+    if (ev) cudaEventDestroy(ev);
+  for (auto &ev : c->ev_split)
     if (ev) cudaEventDestroy(ev);
   *c = trust_tc_ctx();
 }
@@ -90,7 +108,8 @@ struct LaunchCfg {
 static int resolve_cfg(trust_tc_ctx *c, const trust_tc_opts &o, bool same, LaunchCfg *cfg) {
   cfg->threads = o.threads_per_block > 0 ? o.threads_per_block : 256;
   if (cfg->threads % 32 || cfg->threads < 64 || cfg->threads > 1024) return TRUST_TC_E_ARG;
-  cfg->warp_max = o.warp_max_degree > 0 ? o.warp_max_degree : 128;
+  // the plain schedule is the reference's split: a warp per vertex up to out-degree 100 (USE_CTA)
+  cfg->warp_max = o.warp_max_degree > 0 ? o.warp_max_degree : (o.schedule == TRUST_TC_SCHED_PLAIN ? 100 : 128);
   if (cfg->warp_max < 32 || cfg->warp_max > 4096) return TRUST_TC_E_ARG;
   int want_cta = o.block_max_degree > 0 ? o.block_max_degree : 4096;
   if (want_cta < cfg->warp_max) return TRUST_TC_E_ARG;
@@ -111,6 +130,39 @@ static int resolve_cfg(trust_tc_ctx *c, const trust_tc_opts &o, bool same, Launc
   return TRUST_TC_OK;
 }
 
+// The learned schedule promotes a warp-class row to a CTA when its predicted cost exceeds
+// 2^TC_PROMOTE_LOG2 cycles (about half a millisecond at the GB300 clock).
+constexpr float TC_PROMOTE_LOG2 = 20.f;
+
+// Make the cost model in use resident on the device: the caller's (opts.model) or the library's
+// default.  Sets *d_model to null when neither is available (no decisions from a model).
+static int load_model(trust_tc_ctx *c, const float *host_model, const float **d_model) {
+  *d_model = nullptr;
+  float tmp[TC_MODEL_FLOATS];
+  const float *src = host_model;
+  if (!src) {
+    if (trust_tc_model_default(tmp) != TRUST_TC_OK) return TRUST_TC_OK;
+    src = tmp;
+  }
+  int rc = ensure((void **)&c->d_model, &c->model_cap, sizeof(float) * TC_MODEL_FLOATS);
+  if (rc) return rc;
+  if (!c->model_loaded || memcmp(c->model_host, src, sizeof(float) * TC_MODEL_FLOATS) != 0) {
+    memcpy(c->model_host, src, sizeof(float) * TC_MODEL_FLOATS);
+    TC_CUDA_TRY(cudaMemcpy(c->d_model, src, sizeof(float) * TC_MODEL_FLOATS, cudaMemcpyHostToDevice));
+    c->model_loaded = 1;
+  }
+  *d_model = c->d_model;
+  return TRUST_TC_OK;
+}
+
+// Whether the direction split is worth its extra pass over the arcs and the in-list build:
+// enough probes saved in absolute terms (a probe-heavy graph) and relatively.
+static bool split_pays(unsigned long long w_all, unsigned long long w_min, int64_t m, int64_t n) {
+  if (w_all == 0 || m == 0) return false;
+  const double saved = (double)(w_all - w_min);
+  return (double)w_min <= 0.8 * (double)w_all && saved >= 32.0 * (double)(m + n);
+}
+
 // The device-side counting call over three CSRs (A = tables, B = arcs, C = probe lists).
 // `check_*` select which CSRs get an id-range check on the device.
 int count_device(trust_tc_ctx *c, const DevGraph3 &g, const trust_tc_opts &o, bool check_ids,
@@ -124,26 +176,83 @@ int count_device(trust_tc_ctx *c, const DevGraph3 &g, const trust_tc_opts &o, bo
   TC_CUDA_TRY(cudaEventRecord(c->ev[0], st));
   TC_CUDA_TRY(cudaMemsetAsync(ctl, 0, sizeof(TcControl), st));
   // 1. validation of every distinct CSR: offsets always, ids on request
-  rc = launch_check(g.begA, g.adjA, g.rows, g.mA, g.boundA, check_ids, ctl, c->num_sms, st);
+  const int64_t rowsA = g.rowmap ? g.rowsA : g.rows;
+  rc = launch_check(g.begA, g.adjA, rowsA, g.mA, g.boundA, check_ids, ctl, c->num_sms, st);
   if (rc) return rc;
   if (!same) {
     rc = launch_check(g.begB, g.adjB, g.rows, g.mB, g.boundB, check_ids, ctl, c->num_sms, st);
     if (rc) return rc;
-    rc = launch_check(g.begC, g.adjC, g.rowsC, g.mC, g.boundC, check_ids, ctl, c->num_sms, st);
-    if (rc) return rc;
+    if (g.begC != g.begA || g.adjC != g.adjA) {
+      rc = launch_check(g.begC, g.adjC, g.rowsC, g.mC, g.boundC, check_ids, ctl, c->num_sms, st);
+      if (rc) return rc;
+    }
   }
   // 2. classification histogram
   TC_CUDA_TRY(cudaEventRecord(c->ev[1], st));
   ListOffsets off{};
   rc = launch_classify(0, g.begA, g.begB, g.rows, g.min_deg, cfg.warp_max, cfg.cta_max, ctl, c->d_lists,
-                       off, c->num_sms, st);
+                       off, c->num_sms, st, o.schedule, g.rowmap);
   if (rc) return rc;
   TC_CUDA_TRY(cudaMemcpyAsync(c->h_ctl, ctl, sizeof(TcControl), cudaMemcpyDeviceToHost, st));
   TC_CUDA_TRY(cudaStreamSynchronize(st));
-  const TcControl h = *c->h_ctl;
+  TcControl h = *c->h_ctl;
   if (h.status & TC_DEV_BAD_OFFSETS) return TRUST_TC_E_OFFSETS;
   if (h.status & TC_DEV_TOO_LARGE) return TRUST_TC_E_TOO_LARGE;
   if (h.status & TC_DEV_BAD_IDS) return TRUST_TC_E_IDS;
+  // Learned schedule: one scheduling pass over the arcs (split plan, and with a cost model the
+  // predicted cycles and class decision of every row longer than 32), then the direction split
+  // decision; the decisions re-run the class histogram.
+  int split = 0;
+  const unsigned char *dec = nullptr;
+  const float *pred = nullptr;
+  const bool learned = o.schedule == TRUST_TC_SCHED_LEARNED && same && g.min_deg == 2 && g.rows > 0;
+  // the pass is only worth running on skewed rows (short rows bound what it can change)
+  const bool consider = same && g.min_deg == 2 && g.rows > 0 &&
+                        (o.direction_split == 1 || (learned && h.max_out_degree >= 64));
+  if (consider) {
+    const float *d_model = nullptr;
+    if (learned) {
+      rc = load_model(c, o.model, &d_model);
+      if (rc) return rc;
+    }
+    if (o.direction_split != 0) {  // the split needs duplicate-free rows
+      rc = launch_rows_sorted(g.begA, g.adjA, g.rows, ctl, c->num_sms, st);
+      if (rc) return rc;
+    }
+    SchedPlan plan{};
+    rc = split_plan(c, g.begA, g.adjA, g.rows, st, d_model, cfg.warp_max, cfg.cta_max, TC_PROMOTE_LOG2, &plan,
+                    nullptr, cfg.threads / 32);
+    if (rc) return rc;
+    TC_CUDA_TRY(cudaMemcpyAsync(c->h_ctl, ctl, sizeof(TcControl), cudaMemcpyDeviceToHost, st));
+    TC_CUDA_TRY(cudaStreamSynchronize(st));
+    const bool sorted = !(c->h_ctl->status & TC_DEV_UNSORTED);
+    if (o.direction_split == 0) {
+      split = 0;
+    } else if (o.direction_split == 1) {
+      split = sorted;
+    } else if (d_model) {
+      // predicted saving (warp-cycles spread over the resident warps) against the cost of the
+      // in-list build and second-pass setup, with a 1.5x margin
+      const double warps = (double)c->num_sms * (double)std::max(cfg.blocks / std::max(c->num_sms, 1), 1) *
+                           (double)(cfg.threads / 32);
+      const double saved_ms = (double)plan.saved_cycles / (warps * (double)std::max(c->clock_khz, 1));
+      const double cost_ms = 0.05 + 3.5e-8 * (double)g.mA;
+      split = sorted && saved_ms > 1.5 * cost_ms;
+    } else {
+      split = sorted && split_pays(plan.w_all, plan.w_min, g.mA, g.rows);
+    }
+    if (d_model) {
+      dec = c->d_dec;
+      pred = c->d_pred;
+      TC_CUDA_TRY(cudaMemsetAsync(ctl->class_count, 0, sizeof ctl->class_count, st));
+      rc = launch_classify(0, g.begA, g.begB, g.rows, g.min_deg, cfg.warp_max, cfg.cta_max, ctl, c->d_lists, off,
+                           c->num_sms, st, o.schedule, g.rowmap, dec);
+      if (rc) return rc;
+      TC_CUDA_TRY(cudaMemcpyAsync(c->h_ctl, ctl, sizeof(TcControl), cudaMemcpyDeviceToHost, st));
+      TC_CUDA_TRY(cudaStreamSynchronize(st));
+      memcpy(h.class_count, c->h_ctl->class_count, sizeof h.class_count);
+    }
+  }
   int64_t total = 0;
   for (int k = TC_CLASS_SKIP + 1; k < TC_NUM_CLASSES; ++k) {
     off.off[k] = (int)total;
@@ -181,8 +290,12 @@ int count_device(trust_tc_ctx *c, const DevGraph3 &g, const trust_tc_opts &o, bo
   }
   // 3. scatter the class lists
   rc = launch_classify(1, g.begA, g.begB, g.rows, g.min_deg, cfg.warp_max, cfg.cta_max, ctl, c->d_lists,
-                       off, c->num_sms, st);
+                       off, c->num_sms, st, o.schedule, g.rowmap, dec);
   if (rc) return rc;
+  if (pred) {  // heaviest first inside the huge, CTA and warp queues
+    rc = lpt_sort(c, c->d_lists, off.off, h.class_count, pred, st);
+    if (rc) return rc;
+  }
   // 4. count
   a.begA = g.begA; a.begB = g.begB; a.begC = g.begC;
   a.adjA = g.adjA; a.adjB = g.adjB; a.adjC = g.adjC;
@@ -193,6 +306,19 @@ int count_device(trust_tc_ctx *c, const DevGraph3 &g, const trust_tc_opts &o, bo
   a.huge_tables = c->d_huge;
   a.warp_slots = cfg.warp_slots;
   a.chunk = cfg.chunk;
+  a.split = split;
+  a.rowmap = g.rowmap;
+  if (h.class_count[TC_CLASS_CTA] > 0) {
+    // long-row lists: one per CTA, as long as the largest CTA-class row
+    const int cap = (int)std::min<int64_t>(h.max_out_degree, cfg.cta_max);
+    rc = ensure((void **)&c->d_long, &c->long_cap, sizeof(int2) * (size_t)cap * (size_t)blocks);
+    if (rc) return rc;
+    a.long_rows = c->d_long;
+    a.long_cap = cap;
+  }
+  a.cycles = o.record_cycles ? (unsigned long long *)r->vertex_cycles : nullptr;
+  if (o.record_cycles && !r->vertex_cycles) return TRUST_TC_E_ARG;
+  if (a.cycles) TC_CUDA_TRY(cudaMemsetAsync(a.cycles, 0, sizeof(unsigned long long) * (size_t)g.rows, st));
   TC_CUDA_TRY(cudaEventRecord(c->ev[2], st));
   rc = launch_count(same, a, blocks, cfg.threads, smem, st);
   if (rc) return rc;
@@ -213,6 +339,37 @@ int count_device(trust_tc_ctx *c, const DevGraph3 &g, const trust_tc_opts &o, bo
   r->call_seconds = t_call * 1e-3;
   r->max_out_degree = done.max_out_degree;
   for (int k = 0; k < TC_NUM_CLASSES; ++k) r->class_sizes[k] = h.class_count[k];
+  if (split) {
+    // second pass: arcs (v,u) with d(u) > d(v), hashed on u's row, streaming the sources' rows
+    SplitRows sr{};
+    TC_CUDA_TRY(cudaEventRecord(c->ev_split[0], st));
+    rc = split_build(c, g.begA, g.adjA, g.rows, g.mA, st, &sr);
+    if (rc) return rc;
+    TC_CUDA_TRY(cudaEventRecord(c->ev_split[1], st));
+    DevGraph3 gb = g;
+    gb.begB = sr.beg;
+    gb.adjB = sr.adj;
+    gb.mB = sr.m;
+    gb.boundB = g.rows;
+    gb.rowmap = sr.rowmap;
+    gb.rowsA = g.rows;
+    gb.rows = sr.rows;
+    gb.min_deg = 1;
+    trust_tc_opts ob = o;
+    ob.schedule = TRUST_TC_SCHED_TUNED;
+    ob.record_cycles = 0;
+    trust_tc_result rb;
+    memset(&rb, 0, sizeof rb);
+    rc = count_device(c, gb, ob, false, &rb);
+    if (rc) return rc;
+    float t_build = 0;
+    TC_CUDA_TRY(cudaEventElapsedTime(&t_build, c->ev_split[0], c->ev_split[1]));
+    r->triangles += rb.triangles;
+    r->wedges += rb.wedges;
+    r->kernel_seconds += rb.kernel_seconds + t_build * 1e-3;
+    r->count_seconds += rb.count_seconds;
+    r->call_seconds += rb.call_seconds + t_build * 1e-3;
+  }
   return TRUST_TC_OK;
 }
 
@@ -230,8 +387,9 @@ void trust_tc_opts_init(trust_tc_opts *o) {
   memset(o, 0, sizeof *o);
   o->device = -1;
   o->ptr_kind = TRUST_TC_HOST;
-  o->schedule = TRUST_TC_SCHED_PLAIN;
+  o->schedule = TRUST_TC_SCHED_TUNED;
   o->validate = TRUST_TC_VALIDATE_FULL;
+  o->direction_split = -1;
 }
 
 const char *trust_tc_strerror(int s) {
@@ -304,7 +462,8 @@ int trust_tc_count_csr(trust_tc_ctx *ctx, const int64_t *beg, const int32_t *adj
   trust_tc_opts o;
   if (opts) o = *opts; else trust_tc_opts_init(&o);
   if (o.ptr_kind != TRUST_TC_HOST && o.ptr_kind != TRUST_TC_DEVICE) return TRUST_TC_E_ARG;
-  if (o.schedule != TRUST_TC_SCHED_PLAIN && o.schedule != TRUST_TC_SCHED_LEARNED) return TRUST_TC_E_ARG;
+  if (o.schedule != TRUST_TC_SCHED_PLAIN && o.schedule != TRUST_TC_SCHED_LEARNED && o.schedule != TRUST_TC_SCHED_TUNED)
+    return TRUST_TC_E_ARG;
   if (n >= ((int64_t)1 << 31) || m >= ((int64_t)1 << 31)) return TRUST_TC_E_TOO_LARGE;
   uint64_t *cycles = r->vertex_cycles;
   memset(r, 0, sizeof *r);
@@ -402,6 +561,30 @@ int trust_tc_save_folder(const char *folder, const int64_t *beg, const int32_t *
   if (m) ok &= fwrite(adj, sizeof(int32_t), (size_t)m, f) == (size_t)m;
   ok &= fclose(f) == 0;
   return ok ? TRUST_TC_OK : TRUST_TC_E_IO;
+}
+
+int trust_tc_vertex_features(trust_tc_ctx *ctx, const int64_t *d_begin, const int32_t *d_adj, int64_t n, int64_t m,
+                             float *d_features) {
+  if (!ctx || !d_begin || !d_features || n < 0 || m < 0 || (m && !d_adj)) return TRUST_TC_E_ARG;
+  TC_CUDA_TRY(cudaSetDevice(ctx->device));
+  trust_tc_opts o;
+  trust_tc_opts_init(&o);
+  o.ptr_kind = TRUST_TC_DEVICE;
+  LaunchCfg cfg;
+  int rc = resolve_cfg(ctx, o, true, &cfg);
+  if (rc) return rc;
+  // the CSR must be valid before it is walked
+  TC_CUDA_TRY(cudaMemset(ctx->d_ctl, 0, sizeof(TcControl)));
+  rc = launch_check(d_begin, d_adj, n, m, n, 1, ctx->d_ctl, ctx->num_sms, 0);
+  if (rc) return rc;
+  TC_CUDA_TRY(cudaMemcpy(ctx->h_ctl, ctx->d_ctl, sizeof(TcControl), cudaMemcpyDeviceToHost));
+  if (ctx->h_ctl->status & TC_DEV_BAD_OFFSETS) return TRUST_TC_E_OFFSETS;
+  if (ctx->h_ctl->status & TC_DEV_TOO_LARGE) return TRUST_TC_E_TOO_LARGE;
+  if (ctx->h_ctl->status & TC_DEV_BAD_IDS) return TRUST_TC_E_IDS;
+  rc = vertex_features(ctx, d_begin, d_adj, n, cfg.warp_max, cfg.cta_max, d_features, 0);
+  if (rc) return rc;
+  TC_CUDA_TRY(cudaDeviceSynchronize());
+  return TRUST_TC_OK;
 }
 
 int trust_tc_count_folder(const char *folder, const trust_tc_opts *opts, trust_tc_result *r) {

@@ -30,7 +30,8 @@ enum {
   TC_DEV_BAD_IDS = 2,
   TC_DEV_TOO_LARGE = 4,
   TC_DEV_TABLE_FULL = 8,  // a hash insert found no free slot (cannot happen when sized 2x)
-  TC_DEV_WAIT_LIMIT = 16  // a bounded spin wait ran out
+  TC_DEV_WAIT_LIMIT = 16,  // a bounded spin wait ran out
+  TC_DEV_UNSORTED = 32     // informational: some row is not strictly increasing
 };
 
 // Control block living in device scratch.  One per counting call.

@@ -295,9 +295,16 @@ __global__ void check_kernel(const int64_t *__restrict__ beg, const int32_t *__r
   }
 }
 
-__device__ __forceinline__ int classify(int dA, int dB, int min_deg, int warp_max, int cta_max) {
+__device__ __forceinline__ int classify(int dA, int dB, int min_deg, int warp_max, int cta_max, int plain) {
   if (dA < min_deg || dB < min_deg) return TC_CLASS_SKIP;
   int d = max(dA, dB);
+  if (plain) return d <= warp_max ? TC_CLASS_WARP : d <= cta_max ? TC_CLASS_CTA : TC_CLASS_HUGE;
+  if (dA != dB && d > 32) {
+    // tables (A) and arc lists (B) differ: the table size picks warp / CTA / spill table, a long
+    // arc list alone moves the row to a CTA
+    if (dA <= warp_max && dB <= 8 * 32) return TC_CLASS_WARP;
+    return dA <= cta_max ? TC_CLASS_CTA : TC_CLASS_HUGE;
+  }
   if (d <= 4) return TC_CLASS_G4;
   if (d <= 8) return TC_CLASS_G8;
   if (d <= 16) return TC_CLASS_G16;
@@ -310,7 +317,8 @@ __device__ __forceinline__ int classify(int dA, int dB, int min_deg, int warp_ma
 // pass 0: histogram of classes.  pass 1: scatter vertex ids into per-class lists.
 template <int PASS>
 __global__ void class_kernel(const int64_t *__restrict__ begA, const int64_t *__restrict__ begB,
-                             int64_t rows, int min_deg, int warp_max, int cta_max,
+                             int64_t rows, int min_deg, int warp_max, int cta_max, int plain,
+                             const int *__restrict__ rowmap, const unsigned char *__restrict__ dec,
                              TcControl *ctl, int *__restrict__ lists, ListOffsets off) {
   __shared__ int s_hist[TC_NUM_CLASSES];
   __shared__ int s_base[TC_NUM_CLASSES];
@@ -322,9 +330,11 @@ __global__ void class_kernel(const int64_t *__restrict__ begA, const int64_t *__
     int64_t v = base + threadIdx.x;
     int c = -1;
     if (v < rows) {
-      int dA = (int)(tc_ld_nc(begA + v + 1) - tc_ld_nc(begA + v));
-      int dB = (begB == begA) ? dA : (int)(tc_ld_nc(begB + v + 1) - tc_ld_nc(begB + v));
-      c = classify(dA, dB, min_deg, warp_max, cta_max);
+      const int64_t va = rowmap ? (int64_t)rowmap[v] : v;
+      int dA = (int)(tc_ld_nc(begA + va + 1) - tc_ld_nc(begA + va));
+      int dB = (begB == begA && !rowmap) ? dA : (int)(tc_ld_nc(begB + v + 1) - tc_ld_nc(begB + v));
+      c = classify(dA, dB, min_deg, warp_max, cta_max, plain);
+      if (dec && dA == dB && dA > 32) c = dec[v];  // the learned schedule's decision for long rows
     }
     // warp-aggregated block histogram, then one global reservation per class per block
     unsigned peers = __match_any_sync(TC_FULL_MASK, c);
@@ -356,13 +366,44 @@ struct BlockShared {
   unsigned long long wedges;
   int item;
   int next_batch;
+  int n_long;     // deferred long rows of the current CTA vertex
+  int next_long;  // claim head over them
 };
+
+// Neighbour rows at least this long are set aside by the 32-arc batch pass of a CTA vertex and
+// then claimed one row per warp, so one batch full of long rows no longer holds up the CTA.
+constexpr int TC_CTA_LONG = 256;
+
+// Walk one neighbour row with a whole warp: 32 * TC_UNROLL entries per step, next step's loads
+// issued before the current step is probed.
+template <class Set>
+__device__ __forceinline__ void walk_row_warp(const int32_t *__restrict__ row, int dj, int lane, const Set &set,
+                                              unsigned long long &hits) {
+  constexpr int U = TC_UNROLL;
+  int w[U];
+#pragma unroll
+  for (int r = 0; r < U; ++r) w[r] = lane + r * 32 < dj ? tc_ld_nc(row + lane + r * 32) : -1;
+  for (int k = lane; k < dj; k += 32 * U) {
+    const int kn = k + 32 * U;
+    int wn[U];
+#pragma unroll
+    for (int r = 0; r < U; ++r) wn[r] = kn + r * 32 < dj ? tc_ld_nc(row + kn + r * 32) : -1;
+#pragma unroll
+    for (int r = 0; r < U; ++r)
+      if (w[r] >= 0) hits += set.has(w[r]);
+#pragma unroll
+    for (int r = 0; r < U; ++r) w[r] = wn[r];
+  }
+}
 
 __device__ __forceinline__ int ceil_log2_table(int d) {
   // smallest power of two >= 2d, at least 64 slots
   int need = max(2 * d, 64);
   return 32 - __clz(need - 1);
 }
+
+// Table row (in A) of work row v.
+__device__ __forceinline__ int arow(const CountArgs &p, int v) { return p.rowmap ? p.rowmap[v] : v; }
 
 // Row start and length of v (int: m < 2^31 is enforced on the host).
 __device__ __forceinline__ void row_of(const int64_t *__restrict__ beg, int v, int &b, int &d) {
@@ -372,24 +413,31 @@ __device__ __forceinline__ void row_of(const int64_t *__restrict__ beg, int v, i
 }
 
 // One vertex handled by a whole CTA.  `tab` is shared (CTA class) or global (huge class).
-// Warps claim 32-arc batches of the vertex from a shared counter.
+// Pass 1: warps claim 32-arc batches from a shared counter; short rows are flattened and probed
+// at once, rows of TC_CTA_LONG entries or more are appended to this CTA's long-row list (when
+// one is provided and the vertex fits it).  Pass 2: warps claim the long rows one at a time.
 template <bool SAME>
 __device__ void cta_vertex(const CountArgs &p, int v, int *tab, BlockShared &bs, unsigned long long &hits,
                            unsigned long long &wedges) {
   const int lane = threadIdx.x & 31;
   int bA, dA, bB, dB;
-  row_of(p.begA, v, bA, dA);
+  row_of(p.begA, arow(p, v), bA, dA);
   if (SAME) { bB = bA; dB = dA; } else { row_of(p.begB, v, bB, dB); }
   const int log2 = ceil_log2_table(dA);
   const int T = 1 << log2;
   for (int i = threadIdx.x; i < T; i += blockDim.x) tab[i] = -1;
-  if (threadIdx.x == 0) bs.next_batch = 0;
+  if (threadIdx.x == 0) {
+    bs.next_batch = 0;
+    bs.n_long = 0;
+    bs.next_long = 0;
+  }
   __syncthreads();
   bool ok = true;
   for (int i = threadIdx.x; i < dA; i += blockDim.x) ok &= set_insert(tab, log2, tc_ld_nc(p.adjA + bA + i));
   if (!ok) atomicOr(&p.ctl->status, TC_DEV_TABLE_FULL);
   __syncthreads();
   const HashSet set{tab, log2};
+  int2 *longs = (p.long_rows && dB <= p.long_cap) ? p.long_rows + (size_t)blockIdx.x * p.long_cap : nullptr;
   const int nbatch = (dB + 31) >> 5;
   for (;;) {
     int bt = 0;
@@ -399,9 +447,36 @@ __device__ void cta_vertex(const CountArgs &p, int v, int *tab, BlockShared &bs,
     const int i = (bt << 5) + lane;
     int s = 0, dd = 0;
     if (i < dB) row_of(p.begC, tc_ld_nc(p.adjB + bB + i), s, dd);
+    if (SAME && p.split && dd > dB) dd = 0;
+    if (longs) {
+      const bool lg = dd >= TC_CTA_LONG;
+      const unsigned lm = __ballot_sync(TC_FULL_MASK, lg);
+      if (lm) {
+        int at = 0;
+        if (lane == 0) at = atomicAdd(&bs.n_long, __popc(lm));
+        at = __shfl_sync(TC_FULL_MASK, at, 0);
+        if (lg) {
+          longs[at + __popc(lm & tc_lanemask_lt())] = make_int2(s, dd);
+          wedges += (unsigned)dd;
+          dd = 0;
+        }
+      }
+    }
     probe_arcs<32, LongRow<32>::value>(p.adjC, s, dd, lane, set, hits, wedges);
   }
   __syncthreads();
+  if (longs) {
+    const int n_long = bs.n_long;
+    for (;;) {
+      int j = 0;
+      if (lane == 0) j = atomicAdd(&bs.next_long, 1);
+      j = __shfl_sync(TC_FULL_MASK, j, 0);
+      if (j >= n_long) break;
+      const int2 r = longs[j];
+      walk_row_warp(p.adjC + r.x, r.y, lane, set, hits);
+    }
+    __syncthreads();
+  }
 }
 
 // One vertex per warp, 32 < out-degree <= warp_max: several 32-arc rounds on a warp table.
@@ -410,7 +485,7 @@ __device__ __forceinline__ void warp_vertex(const CountArgs &p, int v, int *warp
                                             unsigned long long &wedges) {
   const int lane = threadIdx.x & 31;
   int bA, dA, bB, dB;
-  row_of(p.begA, v, bA, dA);
+  row_of(p.begA, arow(p, v), bA, dA);
   if (SAME) { bB = bA; dB = dA; } else { row_of(p.begB, v, bB, dB); }
   const int log2 = ceil_log2_table(dA);
   const int T = 1 << log2;
@@ -425,6 +500,7 @@ __device__ __forceinline__ void warp_vertex(const CountArgs &p, int v, int *warp
     const int i = a0 + lane;
     int s = 0, dd = 0;
     if (i < dB) row_of(p.begC, tc_ld_nc(p.adjB + bB + i), s, dd);
+    if (SAME && p.split && dd > dB) dd = 0;
     probe_arcs<32, LongRow<32>::value>(p.adjC, s, dd, lane, set, hits, wedges);
   }
   __syncwarp();
@@ -463,7 +539,7 @@ struct GroupStage {
 // Drain one group class.  Each warp claims `chunk` steps of 32/G vertices.  Loads run three
 // steps ahead: while step t is probed, step t+1's target rows, step t+2's row elements and
 // step t+3's row bounds are in flight (the reference walks this chain serially per vertex).
-template <int G, bool SAME>
+template <int G, bool SAME, bool REC>
 __device__ void drain_group_class(const CountArgs &p, int c, int *warp_tab, unsigned long long &hits,
                                   unsigned long long &wedges) {
   constexpr int GPW = 32 / G;
@@ -477,7 +553,7 @@ __device__ void drain_group_class(const CountArgs &p, int c, int *warp_tab, unsi
   auto ld_v = [&](int item, int t1) { return item < t1 ? list[item] : -1; };
   auto ld_row = [&](GroupStage &x) {
     x.b = 0; x.d = 0;
-    if (x.v >= 0) row_of(p.begA, x.v, x.b, x.d);
+    if (x.v >= 0) row_of(p.begA, SAME ? x.v : arow(p, x.v), x.b, x.d);
   };
   auto ld_elem = [&](GroupStage &x) {
     x.uA = glane < x.d ? tc_ld_nc(p.adjA + x.b + glane) : -1;
@@ -492,6 +568,7 @@ __device__ void drain_group_class(const CountArgs &p, int c, int *warp_tab, unsi
   auto ld_target = [&](GroupStage &x) {
     x.s = 0; x.dd = 0;
     if (x.uB >= 0) row_of(p.begC, x.uB, x.s, x.dd);
+    if (SAME && p.split && x.dd > x.d) x.dd = 0;  // counted from u's side in the second pass
   };
   for (;;) {
     int t0 = 0;
@@ -515,7 +592,20 @@ __device__ void drain_group_class(const CountArgs &p, int c, int *warp_tab, unsi
       ld_target(s1);  // row elements of t+1 arrived during the previous step
       ld_elem(s2);
       ld_row(s3);
+      const long long t_start = REC ? clock64() : 0;
       group_vertex<G, SAME>(p, s0.uA, s0.s, s0.dd, warp_tab, hits, wedges);
+      if (REC) {
+        // the step's cycles, shared among its vertices in proportion to their wedges
+        const long long dt = clock64() - t_start;
+        int wv = s0.dd;
+#pragma unroll
+        for (int off = G / 2; off >= 1; off >>= 1) wv += __shfl_xor_sync(TC_FULL_MASK, wv, off, G);
+        int wstep = s0.dd;
+#pragma unroll
+        for (int off = 16; off >= 1; off >>= 1) wstep += __shfl_xor_sync(TC_FULL_MASK, wstep, off);
+        if (glane == 0 && s0.v >= 0)
+          p.cycles[s0.v] = (unsigned long long)(wstep > 0 ? (double)dt * wv / wstep : (double)dt / GPW);
+      }
       s0 = s1;
       s1 = s2;
       s2 = s3;
@@ -527,7 +617,7 @@ __device__ void drain_group_class(const CountArgs &p, int c, int *warp_tab, unsi
 // with at least TC_MIN_CTAS_256 CTAs resident per SM (the default shape).
 constexpr int TC_MIN_CTAS_256 = 5;
 
-template <bool SAME, int MAXT, int MINB>
+template <bool SAME, bool REC, int MAXT, int MINB>
 __global__ void __launch_bounds__(MAXT, MINB) count_kernel(CountArgs p) {
   extern __shared__ int smem[];
   __shared__ BlockShared bs;
@@ -550,7 +640,10 @@ __global__ void __launch_bounds__(MAXT, MINB) count_kernel(CountArgs p) {
       __syncthreads();
       const int t = bs.item;
       if (t >= n_items) break;
-      cta_vertex<SAME>(p, list[t], tab, bs, hits, wedges);
+      const int v = list[t];
+      const long long t_start = REC ? clock64() : 0;
+      cta_vertex<SAME>(p, v, tab, bs, hits, wedges);
+      if (REC && threadIdx.x == 0) p.cycles[v] = (unsigned long long)(clock64() - t_start);
     }
   }
   __syncthreads();
@@ -569,13 +662,18 @@ __global__ void __launch_bounds__(MAXT, MINB) count_kernel(CountArgs p) {
       t0 = __shfl_sync(TC_FULL_MASK, t0, 0);
       if (t0 >= n_items) break;
       const int t1 = min(t0 + claim, n_items);
-      for (int t = t0; t < t1; ++t) warp_vertex<SAME>(p, list[t], warp_tab, hits, wedges);
+      for (int t = t0; t < t1; ++t) {
+        const int v = list[t];
+        const long long t_start = REC ? clock64() : 0;
+        warp_vertex<SAME>(p, v, warp_tab, hits, wedges);
+        if (REC && lane == 0) p.cycles[v] = (unsigned long long)(clock64() - t_start);
+      }
     }
   }
-  drain_group_class<32, SAME>(p, TC_CLASS_G32, warp_tab, hits, wedges);
-  drain_group_class<16, SAME>(p, TC_CLASS_G16, warp_tab, hits, wedges);
-  drain_group_class<8, SAME>(p, TC_CLASS_G8, warp_tab, hits, wedges);
-  drain_group_class<4, SAME>(p, TC_CLASS_G4, warp_tab, hits, wedges);
+  drain_group_class<32, SAME, REC>(p, TC_CLASS_G32, warp_tab, hits, wedges);
+  drain_group_class<16, SAME, REC>(p, TC_CLASS_G16, warp_tab, hits, wedges);
+  drain_group_class<8, SAME, REC>(p, TC_CLASS_G8, warp_tab, hits, wedges);
+  drain_group_class<4, SAME, REC>(p, TC_CLASS_G4, warp_tab, hits, wedges);
 
   // Reduction: warp shuffle -> shared u64 -> one global u64 atomic per CTA
   // (the reference does per-thread shared atomics, Without-graph-partition/TC.cu:586-599).
@@ -606,23 +704,28 @@ int launch_check(const int64_t *beg, const int32_t *adj, int64_t rows, int64_t m
 
 int launch_classify(int pass, const int64_t *begA, const int64_t *begB, int64_t rows, int min_deg,
                     int warp_max, int cta_max, TcControl *ctl, int *lists, const ListOffsets &off,
-                    int num_sms, cudaStream_t st) {
+                    int num_sms, cudaStream_t st, int schedule, const int *rowmap, const unsigned char *dec) {
   int blocks = (int)std::min<int64_t>((rows + 255) / 256, (int64_t)num_sms * 8);
   blocks = std::max(blocks, 1);
+  const int plain = schedule == TRUST_TC_SCHED_PLAIN;
   if (pass == 0)
-    class_kernel<0><<<blocks, 256, 0, st>>>(begA, begB, rows, min_deg, warp_max, cta_max, ctl, lists, off);
+    class_kernel<0><<<blocks, 256, 0, st>>>(begA, begB, rows, min_deg, warp_max, cta_max, plain, rowmap, dec, ctl,
+                                            lists, off);
   else
-    class_kernel<1><<<blocks, 256, 0, st>>>(begA, begB, rows, min_deg, warp_max, cta_max, ctl, lists, off);
+    class_kernel<1><<<blocks, 256, 0, st>>>(begA, begB, rows, min_deg, warp_max, cta_max, plain, rowmap, dec, ctl,
+                                            lists, off);
   TC_CUDA_TRY(cudaGetLastError());
   return TRUST_TC_OK;
 }
 
 template <bool SAME, int MAXT, int MINB>
 static cudaError_t occupancy_of(int threads, size_t smem_bytes, int *blocks_per_sm) {
-  cudaError_t e = cudaFuncSetAttribute(count_kernel<SAME, MAXT, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem_bytes);
+  cudaError_t e = cudaSuccess;
+  for (auto fn : {count_kernel<SAME, false, MAXT, MINB>, count_kernel<SAME, true, MAXT, MINB>}) {
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
+  }
   if (e == cudaSuccess)
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, count_kernel<SAME, MAXT, MINB>, threads,
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, count_kernel<SAME, false, MAXT, MINB>, threads,
                                                       smem_bytes);
   return e;
 }
@@ -641,7 +744,11 @@ int count_kernel_occupancy(bool same, int threads, size_t smem_bytes, int *block
 
 template <bool SAME, int MAXT, int MINB>
 static cudaError_t carveout_of(int pct) {
-  return cudaFuncSetAttribute(count_kernel<SAME, MAXT, MINB>, cudaFuncAttributePreferredSharedMemoryCarveout, pct);
+  cudaError_t e = cudaFuncSetAttribute(count_kernel<SAME, false, MAXT, MINB>,
+                                       cudaFuncAttributePreferredSharedMemoryCarveout, pct);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(count_kernel<SAME, true, MAXT, MINB>, cudaFuncAttributePreferredSharedMemoryCarveout, pct);
+  return e;
 }
 
 int set_count_kernel_carveout(bool same, int threads, size_t smem_bytes, int per_sm) {
@@ -658,18 +765,22 @@ int set_count_kernel_carveout(bool same, int threads, size_t smem_bytes, int per
   return TRUST_TC_OK;
 }
 
+template <bool SAME, int MAXT, int MINB>
+static void launch_one(const CountArgs &a, int blocks, int threads, size_t smem_bytes, cudaStream_t st) {
+  if (a.cycles)
+    count_kernel<SAME, true, MAXT, MINB><<<blocks, threads, smem_bytes, st>>>(a);
+  else
+    count_kernel<SAME, false, MAXT, MINB><<<blocks, threads, smem_bytes, st>>>(a);
+}
+
 int launch_count(bool same, const CountArgs &a, int blocks, int threads, size_t smem_bytes,
                  cudaStream_t st) {
   if (threads <= 256) {
-    if (same)
-      count_kernel<true, 256, TC_MIN_CTAS_256><<<blocks, threads, smem_bytes, st>>>(a);
-    else
-      count_kernel<false, 256, TC_MIN_CTAS_256><<<blocks, threads, smem_bytes, st>>>(a);
+    if (same) launch_one<true, 256, TC_MIN_CTAS_256>(a, blocks, threads, smem_bytes, st);
+    else launch_one<false, 256, TC_MIN_CTAS_256>(a, blocks, threads, smem_bytes, st);
   } else {
-    if (same)
-      count_kernel<true, 1024, 1><<<blocks, threads, smem_bytes, st>>>(a);
-    else
-      count_kernel<false, 1024, 1><<<blocks, threads, smem_bytes, st>>>(a);
+    if (same) launch_one<true, 1024, 1>(a, blocks, threads, smem_bytes, st);
+    else launch_one<false, 1024, 1>(a, blocks, threads, smem_bytes, st);
   }
   TC_CUDA_TRY(cudaGetLastError());
   return TRUST_TC_OK;

@@ -24,13 +24,19 @@ struct CountArgs {
   int huge_blocks;
   int warp_slots;     // shared-memory ints per warp in the warp phase
   int chunk;          // items per queue claim (per group) in the warp phase
+  unsigned long long *cycles;  // optional: per-row clock64 cycles (rows * 1 entries) or null
+  int split;          // 1: skip arcs (v,u) with d(u) > d(v); a second pass counts them from u's side
+  const int *rowmap;  // optional: table row (A) of each work row (B); null = the same index
+  int2 *long_rows;    // optional: per-CTA lists of deferred long neighbour rows (row start, length)
+  int long_cap;       // entries per CTA in long_rows (>= the largest CTA-class out-degree)
 };
 
 int launch_check(const int64_t *beg, const int32_t *adj, int64_t rows, int64_t m, int64_t id_bound,
                  int check_ids, TcControl *ctl, int num_sms, cudaStream_t st);
 int launch_classify(int pass, const int64_t *begA, const int64_t *begB, int64_t rows, int min_deg,
                     int warp_max, int cta_max, TcControl *ctl, int *lists, const ListOffsets &off,
-                    int num_sms, cudaStream_t st);
+                    int num_sms, cudaStream_t st, int schedule = TRUST_TC_SCHED_TUNED,
+                    const int *rowmap = nullptr, const unsigned char *dec = nullptr);
 int count_kernel_occupancy(bool same, int threads, size_t smem_bytes, int *blocks_per_sm);
 // Shared-memory carveout hint: just enough for `per_sm` resident CTAs of `smem_bytes` each.
 int set_count_kernel_carveout(bool same, int threads, size_t smem_bytes, int per_sm);

@@ -17,11 +17,41 @@ struct trust_tc_ctx {
   size_t lists_cap = 0;
   int *d_huge = nullptr;
   size_t huge_cap = 0;
+  int2 *d_long = nullptr;  // per-CTA deferred long-row lists of the CTA class
+  size_t long_cap = 0;
+  unsigned *d_split_cnt = nullptr;  // direction split: in-degree counts / scatter cursors
+  size_t split_cnt_cap = 0;
+  unsigned char *d_dec = nullptr;  // learned schedule: class decision of every row longer than 32
+  size_t dec_cap = 0;
+  float *d_pred = nullptr;  // learned schedule: predicted log2 cycles of those rows
+  size_t pred_cap = 0;
+  float *d_model = nullptr;  // the cost model in use (TC_MODEL_FLOATS)
+  size_t model_cap = 0;
+  float model_host[1400];    // host copy of what d_model holds (reload only on change)
+  int model_loaded = 0;
+  unsigned long long *d_sort = nullptr;  // LPT sort keys and scratch
+  size_t sort_cap = 0;
+  int clock_khz = 0;
+  unsigned long long *d_split_wsum = nullptr;  // per target: probes the second pass makes against it
+  size_t split_wsum_cap = 0;
+  unsigned long long *d_split_plans = nullptr;  // probe totals of both plans
+  size_t split_plans_cap = 0;
+  int64_t *d_split_beg = nullptr;  // in-list offsets of the arcs sent to the second pass
+  size_t split_beg_cap = 0;
+  int64_t *d_split_cbase = nullptr;  // first chunk of every target
+  size_t split_cbase_cap = 0;
+  int64_t *d_split_cbeg = nullptr;  // chunk offsets (the second pass's work rows)
+  size_t split_cbeg_cap = 0;
+  int *d_split_rowmap = nullptr;  // table row of every chunk
+  size_t split_rowmap_cap = 0;
+  int32_t *d_split_adj = nullptr;
+  size_t split_adj_cap = 0;
   int64_t *d_beg = nullptr;
   size_t beg_cap = 0;
   int32_t *d_adj = nullptr;
   size_t adj_cap = 0;
   cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  cudaEvent_t ev_split[2] = {nullptr, nullptr};
 };
 
 namespace tc {
@@ -30,6 +60,8 @@ namespace tc {
 struct DevGraph3 {
   const int64_t *begA, *begB, *begC;
   const int32_t *adjA, *adjB, *adjC;
+  const int *rowmap;          // table row (A) of every work row (B); null = the same index
+  int64_t rowsA;              // rows of A when a row map is given (else = rows)
   int64_t rows;               // rows of A and B
   int64_t rowsC;              // rows of C
   int64_t mA, mB, mC;         // entries of each
@@ -42,5 +74,33 @@ void ctx_release(trust_tc_ctx *c);
 int ensure(void **p, size_t *cap, size_t bytes);
 int count_device(trust_tc_ctx *c, const DevGraph3 &g, const trust_tc_opts &o, bool check_ids,
                  trust_tc_result *r);
+int scan_exclusive_i64(const int64_t *in, int64_t *out, int64_t n, cudaStream_t st, int64_t *total);
+int launch_rows_sorted(const int64_t *beg, const int32_t *adj, int64_t n, TcControl *ctl, int num_sms,
+                       cudaStream_t st);
+struct SchedPlan {
+  unsigned long long w_all, w_min;  // probes without / with the direction split
+  float saved_cycles;               // model: predicted cycles the split saves on rows > 32
+};
+int split_plan(trust_tc_ctx *c, const int64_t *beg, const int32_t *adj, int64_t n, cudaStream_t st,
+               const float *d_model, int warp_max, int cta_max, float promote_log2, SchedPlan *plan,
+               float *d_features, int cta_warps);
+int radix_sort_u64(unsigned long long *keys, unsigned long long *tmp, int64_t n, const int *shifts, int nshifts,
+                   cudaStream_t st);
+// heaviest first: reorder the list of each of the given classes by predicted cycles, descending
+int lpt_sort(trust_tc_ctx *c, int *lists, const int *off, const int *counts, const float *pred, cudaStream_t st);
+int vertex_features(trust_tc_ctx *c, const int64_t *beg, const int32_t *adj, int64_t n, int warp_max,
+                    int cta_max, float *d_features, cudaStream_t st);
+// work rows of the second pass: at least max(TC_SPLIT_WORK_PER_ENTRY * d(u), TC_SPLIT_MIN_WORK)
+// probes each, so the table rebuild stays a small fraction of a row's work
+constexpr int TC_SPLIT_WORK_PER_ENTRY = 256;
+constexpr int TC_SPLIT_MIN_WORK = 131072;
+struct SplitRows {
+  const int64_t *beg;
+  const int32_t *adj;
+  const int *rowmap;
+  int64_t rows, m;
+};
+int split_build(trust_tc_ctx *c, const int64_t *beg, const int32_t *adj, int64_t n, int64_t m, cudaStream_t st,
+                SplitRows *out);
 
 }  // namespace tc

@@ -117,6 +117,10 @@ static int scan_exclusive(const T *in, T *out, int64_t n, cudaStream_t st, T *to
   return TRUST_TC_OK;
 }
 
+int scan_exclusive_i64(const int64_t *in, int64_t *out, int64_t n, cudaStream_t st, int64_t *total) {
+  return scan_exclusive<int64_t>(in, out, n, st, total);
+}
+
 // ------------------------------------------------------------------------------------------
 // stable LSD radix sort of u64 keys, 8-bit digits
 // ------------------------------------------------------------------------------------------
@@ -194,6 +198,11 @@ static int radix_sort(u64 *keys, u64 *tmp, int64_t n, const std::vector<int> &sh
   if (src != keys) TC_CUDA_TRY(cudaMemcpyAsync(keys, src, sizeof(u64) * n, cudaMemcpyDeviceToDevice, st));
   TC_CUDA_TRY(cudaFreeAsync(counts, st));
   return TRUST_TC_OK;
+}
+
+int radix_sort_u64(unsigned long long *keys, unsigned long long *tmp, int64_t n, const int *shifts, int nshifts,
+                   cudaStream_t st) {
+  return radix_sort(keys, tmp, n, std::vector<int>(shifts, shifts + nshifts), st);
 }
 
 static void push_digits(std::vector<int> &v, int lo, int bits) {
