@@ -88,6 +88,8 @@ typedef struct trust_tc_result {
   int64_t wedges;           /* sum over arcs (v,u) with d(v)>=2 of d(u): the probe count     */
   int64_t class_sizes[8];   /* vertices per schedule class (skip, g4, g8, g16, g32, warp, cta, cluster) */
   uint64_t *vertex_cycles;  /* caller-provided device array of n entries, or NULL            */
+  int32_t direction_split;  /* 1 when the second (reverse-direction) pass ran                 */
+  float split_saving_ms;    /* learned schedule: predicted saving of that pass, ms (else 0)  */
 } trust_tc_result;
 
 typedef struct trust_tc_ctx trust_tc_ctx;

@@ -52,12 +52,15 @@ class CountResult:
     max_out_degree: int
     wedges: int = 0
     class_sizes: dict = field(default_factory=dict)
+    direction_split: bool = False
+    split_saving_ms: float = 0.0
 
 
 def _result(r: _lib.Result) -> CountResult:
     return CountResult(int(r.triangles), r.kernel_seconds, r.count_seconds, r.call_seconds, int(r.vertices),
                        int(r.edges), int(r.max_out_degree), int(r.wedges),
-                       {k: int(v) for k, v in zip(CLASS_NAMES, r.class_sizes)})
+                       {k: int(v) for k, v in zip(CLASS_NAMES, r.class_sizes)}, bool(r.direction_split),
+                       float(r.split_saving_ms))
 
 
 def _opts(threads=0, blocks=0, chunk=0, ptr_kind=HOST, validate=VALIDATE_FULL, warp_max=0, block_max=0,

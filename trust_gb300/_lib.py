@@ -48,6 +48,8 @@ class Result(C.Structure):
         ("wedges", C.c_int64),
         ("class_sizes", C.c_int64 * 8),
         ("vertex_cycles", C.c_void_p),
+        ("direction_split", C.c_int32),
+        ("split_saving_ms", C.c_float),
     ]
 
 

@@ -203,6 +203,7 @@ int count_device(trust_tc_ctx *c, const DevGraph3 &g, const trust_tc_opts &o, bo
   // predicted cycles and class decision of every row longer than 32), then the direction split
   // decision; the decisions re-run the class histogram.
   int split = 0;
+  float saving_ms = 0.f;
   const unsigned char *dec = nullptr;
   const float *pred = nullptr;
   const bool learned = o.schedule == TRUST_TC_SCHED_LEARNED && same && g.min_deg == 2 && g.rows > 0;
@@ -237,6 +238,7 @@ int count_device(trust_tc_ctx *c, const DevGraph3 &g, const trust_tc_opts &o, bo
                            (double)(cfg.threads / 32);
       const double saved_ms = (double)plan.saved_cycles / (warps * (double)std::max(c->clock_khz, 1));
       const double cost_ms = 0.05 + 3.5e-8 * (double)g.mA;
+      saving_ms = (float)saved_ms;
       split = sorted && saved_ms > 1.5 * cost_ms;
     } else {
       split = sorted && split_pays(plan.w_all, plan.w_min, g.mA, g.rows);
@@ -339,6 +341,8 @@ int count_device(trust_tc_ctx *c, const DevGraph3 &g, const trust_tc_opts &o, bo
   r->call_seconds = t_call * 1e-3;
   r->max_out_degree = done.max_out_degree;
   for (int k = 0; k < TC_NUM_CLASSES; ++k) r->class_sizes[k] = h.class_count[k];
+  r->direction_split = split;
+  r->split_saving_ms = saving_ms;
   if (split) {
     // second pass: arcs (v,u) with d(u) > d(v), hashed on u's row, streaming the sources' rows
     SplitRows sr{};

@@ -718,11 +718,16 @@ int launch_classify(int pass, const int64_t *begA, const int64_t *begB, int64_t 
   return TRUST_TC_OK;
 }
 
+// The occupancy query honours the kernel's preferred carveout, which a previous call may have
+// set low (a graph needing little shared memory); reset it to the maximum first, or the query
+// (and so the grid) would be limited by the last graph's carveout.
 template <bool SAME, int MAXT, int MINB>
 static cudaError_t occupancy_of(int threads, size_t smem_bytes, int *blocks_per_sm) {
   cudaError_t e = cudaSuccess;
   for (auto fn : {count_kernel<SAME, false, MAXT, MINB>, count_kernel<SAME, true, MAXT, MINB>}) {
     if (e == cudaSuccess) e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
   }
   if (e == cudaSuccess)
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, count_kernel<SAME, false, MAXT, MINB>, threads,

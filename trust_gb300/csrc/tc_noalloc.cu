@@ -92,6 +92,8 @@ extern "C" int trust_tc_count_csr_noalloc(const int64_t *d_begin, const int32_t 
   rc = tc::count_kernel_occupancy(true, threads, smem, &per_sm);
   if (rc) return rc;
   if (per_sm < 1) return TRUST_TC_E_ARG;
+  rc = tc::set_count_kernel_carveout(true, threads, smem, per_sm);
+  if (rc) return rc;
   const int blocks = o.blocks > 0 ? o.blocks : num_sms * per_sm;
 
   cudaStream_t st = (cudaStream_t)o.stream;
@@ -137,5 +139,7 @@ extern "C" int trust_tc_count_csr_noalloc(const int64_t *d_begin, const int32_t 
   r->wedges = (int64_t)done.wedges;
   r->max_out_degree = done.max_out_degree;
   for (int k = 0; k < TC_NUM_CLASSES; ++k) r->class_sizes[k] = h.class_count[k];
+  r->direction_split = 0;
+  r->split_saving_ms = 0.f;
   return TRUST_TC_OK;
 }
