@@ -219,6 +219,7 @@ def test_direction_split(ctx, name):
     for schedule in (T.SCHED_TUNED, T.SCHED_PLAIN, T.SCHED_LEARNED):
         r = T.count_csr(db, da, ctx=ctx, schedule=schedule, direction_split=1)
         assert r.triangles == expect
+        assert r.direction_split
         d = np.diff(beg)
         src = np.repeat(np.arange(d.size), d)
         sel = d[src] >= 2
@@ -226,6 +227,7 @@ def test_direction_split(ctx, name):
     # unsorted rows (the reference preprocess output): the split is not applied, count unchanged
     r = T.count_csr(*_dev(z["ref_beg"], z["ref_adj"]), ctx=ctx, direction_split=1)
     assert r.triangles == expect
+    assert not r.direction_split
     assert r.wedges == O.wedges(z["ref_beg"], z["ref_adj"])
 
 

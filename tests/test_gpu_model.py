@@ -80,13 +80,39 @@ def test_learned_schedule_exact_with_any_model(seed):
         models.append(d)
     with T.Context() as ctx:
         for mod in models:
-            for split in (-1, 0):
+            for split in (-1, 0, 1):
                 r = T.count_csr(beg, adj, ctx=ctx, schedule=T.SCHED_LEARNED, model=mod, direction_split=split)
                 assert r.triangles == expect
         deg = np.diff(b)
+        # (a graph this small only gets the scheduling pass when the split is forced)
         # predicted 2^25 cycles: every warp-class row promoted to a CTA
-        r = T.count_csr(beg, adj, ctx=ctx, schedule=T.SCHED_LEARNED, model=models[1], direction_split=0)
+        r = T.count_csr(beg, adj, ctx=ctx, schedule=T.SCHED_LEARNED, model=models[1], direction_split=1)
         assert r.class_sizes["warp"] == 0 and r.class_sizes["cta"] == int(np.sum((deg > 32) & (deg <= 4096)))
         # predicted 1 cycle: the tuned classes stay
-        r = T.count_csr(beg, adj, ctx=ctx, schedule=T.SCHED_LEARNED, model=models[2], direction_split=0)
+        r = T.count_csr(beg, adj, ctx=ctx, schedule=T.SCHED_LEARNED, model=models[2], direction_split=1)
         assert r.class_sizes["warp"] == int(np.sum((deg > 32) & (deg <= 128)))
+
+
+def test_learned_schedule_gain_on_skewed_rmat():
+    """What the trained network buys over the plain degree-threshold schedule on a skewed graph
+    (R-MAT scale 20, edge factor 16): the same count, the reverse-direction pass chosen from the
+    model's predicted saving, and a shorter call (measured 7.3 ms vs 10.1 ms on GB300; asserted
+    with a wide margin)."""
+    import statistics
+    pairs = T.gen_rmat(20, 16, seed=3)
+    beg, adj = T.build_csr(pairs, 1 << 20)
+    del pairs
+    times = {}
+    counts = {}
+    with T.Context() as ctx:
+        for name, sched in (("plain", T.SCHED_PLAIN), ("learned", T.SCHED_LEARNED)):
+            ts = []
+            for _ in range(5):
+                r = T.count_csr(beg, adj, ctx=ctx, schedule=sched)
+                ts.append(r.call_seconds)
+            times[name] = statistics.median(ts)
+            counts[name] = r.triangles
+            if name == "learned":
+                assert r.direction_split and r.split_saving_ms > 1.0
+    assert counts["learned"] == counts["plain"]
+    assert times["learned"] < 0.85 * times["plain"], times

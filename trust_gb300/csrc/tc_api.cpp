@@ -48,6 +48,7 @@ int ctx_init(trust_tc_ctx *c, int device) {
   TC_CUDA_TRY(cudaDeviceGetAttribute(&c->clock_khz, cudaDevAttrClockRate, device));
   TC_CUDA_TRY(cudaMalloc(&c->d_ctl, sizeof(TcControl)));
   TC_CUDA_TRY(cudaMallocHost(&c->h_ctl, sizeof(TcControl)));
+  TC_CUDA_TRY(cudaMallocHost(&c->h_plans, TC_PLAN_WORDS * sizeof(unsigned long long)));
   for (auto &ev : c->ev) TC_CUDA_TRY(cudaEventCreate(&ev));
   for (auto &ev : c->ev_split) TC_CUDA_TRY(cudaEventCreate(&ev));
   return TRUST_TC_OK;
@@ -57,6 +58,7 @@ void ctx_release(trust_tc_ctx *c) {
   if (c->device >= 0) cudaSetDevice(c->device);
   cudaFree(c->d_ctl);
   cudaFreeHost(c->h_ctl);
+  cudaFreeHost(c->h_plans);
   cudaFree(c->d_lists);
   cudaFree(c->d_huge);
   cudaFree(c->d_long);
@@ -67,6 +69,9 @@ void ctx_release(trust_tc_ctx *c) {
   cudaFree(c->d_sort);
   cudaFree(c->d_split_wsum);
   cudaFree(c->d_split_plans);
+  cudaFree(c->d_sched_long);
+  cudaFree(c->d_split_pairs);
+  cudaFree(c->d_split_ranks);
   cudaFree(c->d_split_beg);
   cudaFree(c->d_split_cbase);
   cudaFree(c->d_split_cbeg);
@@ -133,6 +138,11 @@ static int resolve_cfg(trust_tc_ctx *c, const trust_tc_opts &o, bool same, Launc
 // The learned schedule promotes a warp-class row to a CTA when its predicted cost exceeds
 // 2^TC_PROMOTE_LOG2 cycles (about half a millisecond at the GB300 clock).
 constexpr float TC_PROMOTE_LOG2 = 20.f;
+
+// Below this many arcs the learned schedule's scheduling pass (about 0.1-0.3 ms on GB300) cannot
+// be repaid: the whole count takes about 2 ms or less, and the measured split gain on R-MAT
+// scale 18 (3.8M arcs) is smaller than the pass.  Such graphs run the tuned schedule.
+constexpr int64_t TC_LEARNED_MIN_ARCS = (int64_t)1 << 23;
 
 // Make the cost model in use resident on the device: the caller's (opts.model) or the library's
 // default.  Sets *d_model to null when neither is available (no decisions from a model).
@@ -207,25 +217,35 @@ int count_device(trust_tc_ctx *c, const DevGraph3 &g, const trust_tc_opts &o, bo
   const unsigned char *dec = nullptr;
   const float *pred = nullptr;
   const bool learned = o.schedule == TRUST_TC_SCHED_LEARNED && same && g.min_deg == 2 && g.rows > 0;
-  // the pass is only worth running on skewed rows (short rows bound what it can change)
-  const bool consider = same && g.min_deg == 2 && g.rows > 0 &&
-                        (o.direction_split == 1 || (learned && h.max_out_degree >= 64));
+  // the pass is only worth running on skewed rows (short rows bound what it can change) of a
+  // graph large enough to repay it (it costs about two traversals of the arcs)
+  const bool consider =
+      same && g.min_deg == 2 && g.rows > 0 &&
+      (o.direction_split == 1 || (learned && h.max_out_degree >= 64 && g.mA >= TC_LEARNED_MIN_ARCS));
   if (consider) {
     const float *d_model = nullptr;
     if (learned) {
       rc = load_model(c, o.model, &d_model);
       if (rc) return rc;
     }
-    if (o.direction_split != 0) {  // the split needs duplicate-free rows
-      rc = launch_rows_sorted(g.begA, g.adjA, g.rows, ctl, c->num_sms, st);
+    // (the pass also checks that rows are duplicate-free, which the split needs); with a model,
+    // the class histogram under its decisions follows on the stream before the one readback
+    rc = split_plan(c, g.begA, g.adjA, g.rows, g.mA, st, d_model, cfg.warp_max, cfg.cta_max, TC_PROMOTE_LOG2,
+                    cfg.threads / 32, ctl);
+    if (rc) return rc;
+    if (d_model) {
+      dec = c->d_dec;
+      pred = c->d_pred;
+      TC_CUDA_TRY(cudaMemsetAsync(ctl->class_count, 0, sizeof ctl->class_count, st));
+      rc = launch_classify(0, g.begA, g.begB, g.rows, g.min_deg, cfg.warp_max, cfg.cta_max, ctl, c->d_lists, off,
+                           c->num_sms, st, o.schedule, g.rowmap, dec);
       if (rc) return rc;
     }
-    SchedPlan plan{};
-    rc = split_plan(c, g.begA, g.adjA, g.rows, st, d_model, cfg.warp_max, cfg.cta_max, TC_PROMOTE_LOG2, &plan,
-                    nullptr, cfg.threads / 32);
-    if (rc) return rc;
     TC_CUDA_TRY(cudaMemcpyAsync(c->h_ctl, ctl, sizeof(TcControl), cudaMemcpyDeviceToHost, st));
     TC_CUDA_TRY(cudaStreamSynchronize(st));
+    SchedPlan plan{};
+    split_plan_read(c, &plan);
+    if (d_model) memcpy(h.class_count, c->h_ctl->class_count, sizeof h.class_count);
     const bool sorted = !(c->h_ctl->status & TC_DEV_UNSORTED);
     if (o.direction_split == 0) {
       split = 0;
@@ -242,17 +262,6 @@ int count_device(trust_tc_ctx *c, const DevGraph3 &g, const trust_tc_opts &o, bo
       split = sorted && saved_ms > 1.5 * cost_ms;
     } else {
       split = sorted && split_pays(plan.w_all, plan.w_min, g.mA, g.rows);
-    }
-    if (d_model) {
-      dec = c->d_dec;
-      pred = c->d_pred;
-      TC_CUDA_TRY(cudaMemsetAsync(ctl->class_count, 0, sizeof ctl->class_count, st));
-      rc = launch_classify(0, g.begA, g.begB, g.rows, g.min_deg, cfg.warp_max, cfg.cta_max, ctl, c->d_lists, off,
-                           c->num_sms, st, o.schedule, g.rowmap, dec);
-      if (rc) return rc;
-      TC_CUDA_TRY(cudaMemcpyAsync(c->h_ctl, ctl, sizeof(TcControl), cudaMemcpyDeviceToHost, st));
-      TC_CUDA_TRY(cudaStreamSynchronize(st));
-      memcpy(h.class_count, c->h_ctl->class_count, sizeof h.class_count);
     }
   }
   int64_t total = 0;

@@ -29,13 +29,20 @@ struct trust_tc_ctx {
   size_t model_cap = 0;
   float model_host[1400];    // host copy of what d_model holds (reload only on change)
   int model_loaded = 0;
-  unsigned long long *d_sort = nullptr;  // LPT sort keys and scratch
+  unsigned long long *d_sort = nullptr;  // heaviest-first sort: histogram, cursors, sorted copy
   size_t sort_cap = 0;
   int clock_khz = 0;
   unsigned long long *d_split_wsum = nullptr;  // per target: probes the second pass makes against it
   size_t split_wsum_cap = 0;
-  unsigned long long *d_split_plans = nullptr;  // probe totals of both plans
+  unsigned long long *d_split_plans = nullptr;  // probe totals of both plans, saving, long rows
   size_t split_plans_cap = 0;
+  unsigned long long *h_plans = nullptr;        // pinned host copy of d_split_plans
+  int2 *d_split_pairs = nullptr;  // scheduling pass: the arcs the split would move, (target, source)
+  size_t split_pairs_cap = 0;
+  unsigned *d_split_ranks = nullptr;  // and each one's slot in its target's in-list
+  size_t split_ranks_cap = 0;
+  int *d_sched_long = nullptr;  // scheduling pass: the rows it walks a warp each
+  size_t sched_long_cap = 0;
   int64_t *d_split_beg = nullptr;  // in-list offsets of the arcs sent to the second pass
   size_t split_beg_cap = 0;
   int64_t *d_split_cbase = nullptr;  // first chunk of every target
@@ -75,15 +82,17 @@ int ensure(void **p, size_t *cap, size_t bytes);
 int count_device(trust_tc_ctx *c, const DevGraph3 &g, const trust_tc_opts &o, bool check_ids,
                  trust_tc_result *r);
 int scan_exclusive_i64(const int64_t *in, int64_t *out, int64_t n, cudaStream_t st, int64_t *total);
-int launch_rows_sorted(const int64_t *beg, const int32_t *adj, int64_t n, TcControl *ctl, int num_sms,
-                       cudaStream_t st);
+constexpr int TC_PLAN_WORDS = 8;  // words of the scheduling pass's totals
 struct SchedPlan {
   unsigned long long w_all, w_min;  // probes without / with the direction split
   float saved_cycles;               // model: predicted cycles the split saves on rows > 32
+  int64_t long_rows;                // rows longer than 32 entries
+  int64_t moved_arcs;               // arcs the split sends to the second pass
 };
-int split_plan(trust_tc_ctx *c, const int64_t *beg, const int32_t *adj, int64_t n, cudaStream_t st,
-               const float *d_model, int warp_max, int cta_max, float promote_log2, SchedPlan *plan,
-               float *d_features, int cta_warps);
+int split_plan(trust_tc_ctx *c, const int64_t *beg, const int32_t *adj, int64_t n, int64_t m, cudaStream_t st,
+               const float *d_model, int warp_max, int cta_max, float promote_log2, int cta_warps, TcControl *ctl);
+// after the stream has synchronised
+void split_plan_read(const trust_tc_ctx *c, SchedPlan *plan);
 int radix_sort_u64(unsigned long long *keys, unsigned long long *tmp, int64_t n, const int *shifts, int nshifts,
                    cudaStream_t st);
 // heaviest first: reorder the list of each of the given classes by predicted cycles, descending

@@ -20,21 +20,6 @@
 
 namespace tc {
 
-// Rows strictly increasing (sorted, no duplicates)?  Clears nothing; sets TC_DEV_UNSORTED.
-__global__ void rows_sorted_kernel(const int64_t *__restrict__ beg, const int32_t *__restrict__ adj, int64_t n,
-                                   TcControl *ctl) {
-  const int lane = threadIdx.x & 31;
-  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  int bad = 0;
-  for (int64_t v = warp; v < n; v += nwarps) {
-    const int64_t b = tc_ld_nc(beg + v), e = tc_ld_nc(beg + v + 1);
-    for (int64_t i = b + lane; i + 1 < e; i += 32) bad |= tc_ld_nc(adj + i) >= tc_ld_nc(adj + i + 1);
-  }
-  bad = __reduce_or_sync(TC_FULL_MASK, bad);
-  if (lane == 0 && bad) atomicOr(&ctl->status, TC_DEV_UNSORTED);
-}
-
 // Position (0..31) of the n-th (0-based) set bit of mask; mask must have more than n set bits.
 __device__ __forceinline__ int split_nth_bit(unsigned mask, int n) {
   int pos = 0;
@@ -50,14 +35,22 @@ __device__ __forceinline__ int split_nth_bit(unsigned mask, int n) {
   return pos;
 }
 
-// Visit every arc (v,u) with d(v) >= 2 as f(v, d(v), u, d(u)).  A warp takes 32 consecutive
-// vertices; rows of up to SPLIT_FLAT entries are flattened into one list over the 32 lanes
-// (coalesced row reads, every lane's neighbour-degree loads independent), longer rows are walked
-// by the whole warp.
-constexpr int SPLIT_FLAT = 128;
+// ---- traversal of the arcs ---------------------------------------------------------------------
+// Every arc (v,u) with d(v) >= 2 is visited once, in two phases.  Phase 1: a warp takes 32
+// consecutive vertices and flattens their rows of 2..TC_SCHED_FLAT entries into one list over
+// the lanes (coalesced row reads, independent neighbour-degree loads); longer rows are appended
+// to a list.  Phase 2: one warp per listed row, rows dealt round-robin over the warps, four
+// 32-entry steps of loads in flight.  No warp walks a whole tile of long rows (after renumbering
+// by out-degree the first tiles hold the longest rows of the graph).
+constexpr int TC_SCHED_FLAT = 32;
+
+// Phase 1.  f(valid, v, d(v), u, d(u), pos, last) is called by all 32 lanes together (warp
+// collectives allowed); lanes with valid = false carry no arc.  pos = the arc's index in adj,
+// last = it ends its row.  Rows longer than TC_SCHED_FLAT are appended to longs[] (length in
+// *nlong) when longs is given.
 template <class F>
-__device__ __forceinline__ void for_each_arc(const int64_t *__restrict__ beg, const int32_t *__restrict__ adj,
-                                             int64_t n, F f) {
+__device__ __forceinline__ void short_arcs(const int64_t *__restrict__ beg, const int32_t *__restrict__ adj,
+                                           int64_t n, int *__restrict__ longs, unsigned long long *nlong, F f) {
   const int lane = threadIdx.x & 31;
   const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -70,20 +63,17 @@ __device__ __forceinline__ void for_each_arc(const int64_t *__restrict__ beg, co
       b = (int)lo;
       dv = (int)(tc_ld_nc(beg + v + 1) - lo);
     }
-    const int sd = (dv >= 2 && dv <= SPLIT_FLAT) ? dv : 0;
-    // long rows
-    unsigned big = __ballot_sync(TC_FULL_MASK, dv > SPLIT_FLAT);
-    while (big) {
-      const int j = __ffs(big) - 1;
-      big &= big - 1;
-      const int bj = __shfl_sync(TC_FULL_MASK, b, j);
-      const int dj = __shfl_sync(TC_FULL_MASK, dv, j);
-      for (int i = lane; i < dj; i += 32) {
-        const int u = tc_ld_nc(adj + bj + i);
-        f((int)(v0 + j), dj, u, (int)(tc_ld_nc(beg + u + 1) - tc_ld_nc(beg + u)));
+    if (longs) {
+      const unsigned big = __ballot_sync(TC_FULL_MASK, dv > TC_SCHED_FLAT);
+      if (big) {
+        unsigned long long at = 0;
+        if (lane == 0) at = atomicAdd(nlong, (unsigned long long)__popc(big));
+        at = __shfl_sync(TC_FULL_MASK, at, 0);
+        if (dv > TC_SCHED_FLAT) longs[at + __popc(big & (upto >> 1))] = (int)v;
       }
     }
-    // short rows, flattened: ranked nonempty rows, owner of a slot from the start-bit mask
+    // ranked nonempty rows; the owner of a slot comes from the start-bit mask
+    const int sd = (dv >= 2 && dv <= TC_SCHED_FLAT) ? dv : 0;
     int incl = sd;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -107,23 +97,86 @@ __device__ __forceinline__ void for_each_arc(const int64_t *__restrict__ beg, co
       before += __popc(starts);
       const int base = __shfl_sync(TC_FULL_MASK, cbase, c);
       const int deg = __shfl_sync(TC_FULL_MASK, cdeg, c);
+      const int ex = __shfl_sync(TC_FULL_MASK, cexcl, c);
       const int row = __shfl_sync(TC_FULL_MASK, src, c);
       const int k = k0 + lane;
-      if (k < tot) {
-        const int u = tc_ld_nc(adj + base + k);
-        f((int)(v0 + row), deg, u, (int)(tc_ld_nc(beg + u + 1) - tc_ld_nc(beg + u)));
+      const bool valid = k < tot;
+      const int pos = base + k;
+      int u = 0, du = 0;
+      if (valid) {
+        u = tc_ld_nc(adj + pos);
+        du = (int)(tc_ld_nc(beg + u + 1) - tc_ld_nc(beg + u));
       }
+      f(valid, (int)(v0 + row), deg, u, du, pos, k + 1 == ex + deg);
     }
   }
 }
 
-// Scatter the sources of the second-pass arcs into their targets' in-lists.
-__global__ void split_fill_kernel(const int64_t *__restrict__ beg, const int32_t *__restrict__ adj, int64_t n,
-                                  unsigned *__restrict__ cursor, const int64_t *__restrict__ off,
+// Phase 2 for one row (entries adj[b, b+dv)) by a whole warp: f(valid, u, d(u), pos, last), called
+// by all lanes together as in phase 1.
+template <class F>
+__device__ __forceinline__ void long_row_arcs(const int64_t *__restrict__ beg, const int32_t *__restrict__ adj,
+                                              int b, int dv, int lane, F f) {
+  for (int i0 = 0; i0 < dv; i0 += 128) {
+    int u[4], du[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int i = i0 + 32 * k + lane;
+      u[k] = i < dv ? tc_ld_nc(adj + b + i) : -1;
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) du[k] = u[k] >= 0 ? (int)(tc_ld_nc(beg + u[k] + 1) - tc_ld_nc(beg + u[k])) : 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int i = i0 + 32 * k + lane;
+      f(i < dv, u[k], du[k], b + i, i == dv - 1);
+    }
+  }
+}
+
+// An arc (v,u) the split would move (mv): count it in u's in-list (cnt) and work sum (wsum) and
+// append it as a (target, source) pair with its slot in u's in-list (the rank the count returns),
+// so the in-lists are later filled without atomics.  Called by all 32 lanes together; lanes that
+// move an arc to the same target share one atomic (hub targets receive many).
+__device__ __forceinline__ void move_arc(bool mv, int u, int v, int dv, unsigned *__restrict__ cnt,
+                                         unsigned long long *__restrict__ wsum, int2 *__restrict__ pairs,
+                                         unsigned *__restrict__ ranks, unsigned long long *npairs) {
+  const unsigned m = __ballot_sync(TC_FULL_MASK, mv);
+  if (!m) return;
+  const int lane = threadIdx.x & 31;
+  const unsigned lt = tc_lanemask_lt();
+  const unsigned peers = __match_any_sync(TC_FULL_MASK, mv ? u : -1);
+  unsigned rank = 0;
+  if (mv) {
+    const int leader = __ffs(peers) - 1;
+    const unsigned sum = __reduce_add_sync(peers, (unsigned)dv);
+    unsigned base = 0;
+    if (lane == leader) {
+      base = atomicAdd(cnt + u, (unsigned)__popc(peers));
+      atomicAdd(wsum + u, (unsigned long long)sum);
+    }
+    base = __shfl_sync(peers, base, leader);
+    rank = base + __popc(peers & lt);
+  }
+  unsigned long long at = 0;
+  if (lane == 0) at = atomicAdd(npairs, (unsigned long long)__popc(m));
+  at = __shfl_sync(TC_FULL_MASK, at, 0);
+  if (mv) {
+    const unsigned long long k = at + __popc(m & lt);
+    pairs[k] = make_int2(u, v);
+    ranks[k] = rank;
+  }
+}
+
+// Fill the in-lists: every pair's source goes to its recorded slot.
+__global__ void split_fill_kernel(const int2 *__restrict__ pairs, const unsigned *__restrict__ ranks,
+                                  const unsigned long long *__restrict__ npairs, const int64_t *__restrict__ off,
                                   int32_t *__restrict__ adj_b) {
-  for_each_arc(beg, adj, n, [&](int v, int dv, int u, int du) {
-    if (du > dv) adj_b[off[u] + atomicAdd(cursor + u, 1u)] = v;
-  });
+  const int64_t np = (int64_t)*npairs;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < np; i += (int64_t)gridDim.x * blockDim.x) {
+    const int2 p = pairs[i];
+    adj_b[off[p.x] + ranks[i]] = p.y;
+  }
 }
 
 // ---- the learned schedule's scheduling pass ----------------------------------------------------
@@ -178,16 +231,53 @@ __device__ __forceinline__ int tuned_class_of(int d, int warp_max, int cta_max) 
   return d <= cta_max ? TC_CLASS_CTA : TC_CLASS_HUGE;
 }
 
-// One traversal: the split plan's totals and in-list counts for every arc, and for every row
-// longer than 32 its features, its predicted cycles (model) and its class decision: a warp-class
-// row predicted to cost more than 2^promote_log2 cycles is promoted to a CTA.  sums[0] collects
-// the predicted cycles the split would save (each row's prediction times its probe saving).
+// Words of the scheduling pass's totals (plans[]).
+enum { PLAN_W_ALL = 0, PLAN_W_MIN = 1, PLAN_SAVED = 2, PLAN_NLONG = 3, PLAN_NPAIRS = 4 };
+
+// The scheduling pass, phase 1 (rows of up to TC_SCHED_FLAT entries): the split plan's probe
+// totals, the in-list count and work sum of every arc's target, the arcs the split would move
+// (as pairs), and the sortedness check; rows longer than TC_SCHED_FLAT are listed.
+__global__ void sched_short_kernel(const int64_t *__restrict__ beg, const int32_t *__restrict__ adj, int64_t n,
+                                   unsigned *__restrict__ cnt, unsigned long long *__restrict__ wsum,
+                                   unsigned long long *plans, int *__restrict__ longs, int2 *__restrict__ pairs,
+                                   unsigned *__restrict__ ranks, TcControl *ctl) {
+  const int lane = threadIdx.x & 31;
+  unsigned long long w_all = 0, w_min = 0;
+  int bad = 0;
+  short_arcs(beg, adj, n, longs, plans + PLAN_NLONG,
+             [&](bool valid, int v, int dv, int u, int du, int pos, bool last) {
+               if (valid) {
+                 w_all += (unsigned)du;
+                 w_min += (unsigned)min(du, dv);
+                 if (!last) bad |= u >= tc_ld_nc(adj + pos + 1);
+               }
+               move_arc(valid && du > dv, u, v, dv, cnt, wsum, pairs, ranks, plans + PLAN_NPAIRS);
+             });
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) {
+    w_all += __shfl_down_sync(TC_FULL_MASK, w_all, o);
+    w_min += __shfl_down_sync(TC_FULL_MASK, w_min, o);
+  }
+  bad = __reduce_or_sync(TC_FULL_MASK, bad);
+  if (lane == 0) {
+    if (w_all) atomicAdd(plans + PLAN_W_ALL, w_all);
+    if (w_min) atomicAdd(plans + PLAN_W_MIN, w_min);
+    if (bad) atomicOr(&ctl->status, TC_DEV_UNSORTED);
+  }
+}
+
+// Phase 2 (the listed rows, a warp each): the same totals, counts and check, plus every row's
+// features and, with a model, its predicted cycles and class decision: a warp-class row
+// predicted to cost more than 2^promote_log2 cycles is promoted to a CTA.  sums[0] collects the
+// predicted cycles the split would save (each row's prediction times its probe saving).
 template <bool MODEL>
-__global__ void sched_kernel(const int64_t *__restrict__ beg, const int32_t *__restrict__ adj, int64_t n,
-                             unsigned *__restrict__ cnt, unsigned long long *__restrict__ wsum,
-                             unsigned long long *plans, const float *__restrict__ model, int warp_max, int cta_max,
-                             float promote_log2, unsigned char *__restrict__ dec, float *__restrict__ pred,
-                             float *sums, float *__restrict__ feats, int cta_warps) {
+__global__ void sched_long_kernel(const int64_t *__restrict__ beg, const int32_t *__restrict__ adj,
+                                  unsigned *__restrict__ cnt, unsigned long long *__restrict__ wsum,
+                                  unsigned long long *plans, const int *__restrict__ longs,
+                                  const float *__restrict__ model, int warp_max, int cta_max, float promote_log2,
+                                  unsigned char *__restrict__ dec, float *__restrict__ pred, float *sums,
+                                  int cta_warps, int2 *__restrict__ pairs, unsigned *__restrict__ ranks,
+                                  TcControl *ctl) {
   __shared__ float P[MODEL ? TC_MODEL_FLOATS : 1];
   if (MODEL) {  // staged with W1 and W2 transposed (see warp_mlp)
     for (int i = threadIdx.x; i < TC_MODEL_FLOATS; i += blockDim.x) {
@@ -207,114 +297,60 @@ __global__ void sched_kernel(const int64_t *__restrict__ beg, const int32_t *__r
   const int lane = threadIdx.x & 31;
   const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  const unsigned upto = 0xffffffffu >> (31 - lane);
+  const int64_t nl = (int64_t)plans[PLAN_NLONG];
   unsigned long long w_all = 0, w_min = 0;
   float saved = 0.f;
-  for (int64_t v0 = warp * 32; v0 < n; v0 += nwarps * 32) {
-    const int64_t v = v0 + lane;
-    int b = 0, dv = 0;
-    if (v < n) {
-      const long long lo = tc_ld_nc(beg + v);
-      b = (int)lo;
-      dv = (int)(tc_ld_nc(beg + v + 1) - lo);
-    }
-    // rows longer than 32: a warp each, with features and the model
-    unsigned big = __ballot_sync(TC_FULL_MASK, dv > 32);
-    while (big) {
-      const int j = __ffs(big) - 1;
-      big &= big - 1;
-      const int bj = __shfl_sync(TC_FULL_MASK, b, j);
-      const int dj = __shfl_sync(TC_FULL_MASK, dv, j);
-      unsigned long long rw = 0, rmin = 0;
-      int rmax = 0, rnb = 0;
-      for (int i = lane; i < dj; i += 32) {
-        const int u = tc_ld_nc(adj + bj + i);
-        const int du = (int)(tc_ld_nc(beg + u + 1) - tc_ld_nc(beg + u));
+  int bad = 0;
+  for (int64_t idx = warp; idx < nl; idx += nwarps) {
+    const int v = longs[idx];
+    const long long lo = tc_ld_nc(beg + v);
+    const int dv = (int)(tc_ld_nc(beg + v + 1) - lo);
+    unsigned long long rw = 0, rmin = 0;
+    int rmax = 0, rnb = 0;
+    long_row_arcs(beg, adj, (int)lo, dv, lane, [&](bool valid, int u, int du, int pos, bool last) {
+      const bool mv = valid && du > dv;
+      if (valid) {
         rw += (unsigned)du;
-        rmin += (unsigned)min(du, dj);
+        rmin += (unsigned)min(du, dv);
         rmax = max(rmax, du);
-        if (du > dj) {
-          ++rnb;
-          atomicAdd(cnt + u, 1u);
-          atomicAdd(wsum + u, (unsigned long long)dj);
-        }
+        rnb += mv;
+        if (!last) bad |= u >= tc_ld_nc(adj + pos + 1);
       }
+      move_arc(mv, u, v, dv, cnt, wsum, pairs, ranks, plans + PLAN_NPAIRS);
+    });
 #pragma unroll
-      for (int o = 16; o >= 1; o >>= 1) {
-        rw += __shfl_xor_sync(TC_FULL_MASK, rw, o);
-        rmin += __shfl_xor_sync(TC_FULL_MASK, rmin, o);
-        rmax = max(rmax, __shfl_xor_sync(TC_FULL_MASK, rmax, o));
-        rnb += __shfl_xor_sync(TC_FULL_MASK, rnb, o);
-      }
-      if (lane == 0) {
-        w_all += rw;
-        w_min += rmin;
-      }
-      const int cls = tuned_class_of(dj, warp_max, cta_max);
+    for (int o = 16; o >= 1; o >>= 1) {
+      rw += __shfl_xor_sync(TC_FULL_MASK, rw, o);
+      rmin += __shfl_xor_sync(TC_FULL_MASK, rmin, o);
+      rmax = max(rmax, __shfl_xor_sync(TC_FULL_MASK, rmax, o));
+      rnb += __shfl_xor_sync(TC_FULL_MASK, rnb, o);
+    }
+    if (lane == 0) {
+      w_all += rw;
+      w_min += rmin;
+    }
+    if (MODEL) {
+      const int cls = tuned_class_of(dv, warp_max, cta_max);
       float f[TC_FEATURES];
-      row_features(f, dj, rw, rmin, rmax, rnb, cls);
-      if (feats && lane < TC_FEATURES) feats[(v0 + j) * TC_FEATURES + lane] = f[lane];
-      if (MODEL) {
-        const float y = warp_mlp(P, f, lane);
-        if (lane == 0) {
-          int d = cls;
-          if (d == TC_CLASS_WARP && y > promote_log2) d = TC_CLASS_CTA;
-          dec[v0 + j] = (unsigned char)d;
-          pred[v0 + j] = y;
-          // warp-cycles: a CTA row's cycles are spent by all its warps
-          const float warps = d >= TC_CLASS_CTA ? (float)cta_warps : 1.f;
-          if (rw > 0) saved += warps * exp2f(fminf(y, 60.f)) * (float)((double)(rw - rmin) / (double)rw);
-        }
-      }
-    }
-    // rows of 2..32 entries: flattened over the warp (split totals and counts only)
-    const int sd = (dv >= 2 && dv <= 32) ? dv : 0;
-    int incl = sd;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const int y = __shfl_up_sync(TC_FULL_MASK, incl, o);
-      if (lane >= o) incl += y;
-    }
-    const int tot = __shfl_sync(TC_FULL_MASK, incl, 31);
-    if (tot == 0) continue;
-    const unsigned ne = __ballot_sync(TC_FULL_MASK, sd > 0);
-    const int nc = __popc(ne);
-    const int src = lane < nc ? split_nth_bit(ne, lane) : 0;
-    const int src_excl = __shfl_sync(TC_FULL_MASK, incl - sd, src);
-    const int cexcl = lane < nc ? src_excl : 0x7fffffff;
-    const int cbase = __shfl_sync(TC_FULL_MASK, b - (incl - sd), src);
-    const int cdeg = __shfl_sync(TC_FULL_MASK, sd, src);
-    int before = 0;
-    for (int k0 = 0; k0 < tot; k0 += 32) {
-      const unsigned starts =
-          __reduce_or_sync(TC_FULL_MASK, (cexcl >= k0 && cexcl < k0 + 32) ? (1u << (cexcl - k0)) : 0u);
-      const int c = max(before + __popc(starts & upto) - 1, 0);
-      before += __popc(starts);
-      const int base = __shfl_sync(TC_FULL_MASK, cbase, c);
-      const int deg = __shfl_sync(TC_FULL_MASK, cdeg, c);
-      const int k = k0 + lane;
-      if (k < tot) {
-        const int u = tc_ld_nc(adj + base + k);
-        const int du = (int)(tc_ld_nc(beg + u + 1) - tc_ld_nc(beg + u));
-        w_all += (unsigned)du;
-        w_min += (unsigned)min(du, deg);
-        if (du > deg) {
-          atomicAdd(cnt + u, 1u);
-          atomicAdd(wsum + u, (unsigned long long)deg);
-        }
+      row_features(f, dv, rw, rmin, rmax, rnb, cls);
+      const float y = warp_mlp(P, f, lane);
+      if (lane == 0) {
+        int d = cls;
+        if (d == TC_CLASS_WARP && y > promote_log2) d = TC_CLASS_CTA;
+        dec[v] = (unsigned char)d;
+        pred[v] = y;
+        // warp-cycles: a CTA row's cycles are spent by all its warps
+        const float warps = d >= TC_CLASS_CTA ? (float)cta_warps : 1.f;
+        if (rw > 0) saved += warps * exp2f(fminf(y, 60.f)) * (float)((double)(rw - rmin) / (double)rw);
       }
     }
   }
-#pragma unroll
-  for (int o = 16; o >= 1; o >>= 1) {
-    w_all += __shfl_down_sync(TC_FULL_MASK, w_all, o);
-    w_min += __shfl_down_sync(TC_FULL_MASK, w_min, o);
-    saved += __shfl_down_sync(TC_FULL_MASK, saved, o);
-  }
+  bad = __reduce_or_sync(TC_FULL_MASK, bad);
   if (lane == 0) {
-    atomicAdd(plans + 0, w_all);
-    atomicAdd(plans + 1, w_min);
+    if (w_all) atomicAdd(plans + PLAN_W_ALL, w_all);
+    if (w_min) atomicAdd(plans + PLAN_W_MIN, w_min);
     if (MODEL && saved > 0.f) atomicAdd(sums, saved);
+    if (bad) atomicOr(&ctl->status, TC_DEV_UNSORTED);
   }
 }
 
@@ -360,60 +396,67 @@ __global__ void chunk_fill_kernel(const int64_t *__restrict__ cbase, const int64
   if (blockIdx.x == 0 && threadIdx.x == 0) cbeg[nchunks] = total;
 }
 
-int launch_rows_sorted(const int64_t *beg, const int32_t *adj, int64_t n, TcControl *ctl, int num_sms, cudaStream_t st) {
-  int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((n * 32 + 255) / 256, (int64_t)num_sms * 8));
-  rows_sorted_kernel<<<blocks, 256, 0, st>>>(beg, adj, n, ctl);
-  TC_CUDA_TRY(cudaGetLastError());
-  return TRUST_TC_OK;
-}
-
 static int arc_blocks(int64_t n, int num_sms) {  // one warp per 32 vertices
   return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)num_sms * 16));
 }
 
-// The scheduling pass (one traversal of the arcs): probe totals of both plans, the split's
-// in-degree counts and work sums, and - with a model - every long row's predicted cycles and
-// class decision plus the predicted saving of the split (SchedPlan).
-int split_plan(trust_tc_ctx *c, const int64_t *beg, const int32_t *adj, int64_t n, cudaStream_t st,
-               const float *d_model, int warp_max, int cta_max, float promote_log2, SchedPlan *plan,
-               float *d_features, int cta_warps) {
-  int rc = ensure((void **)&c->d_split_cnt, &c->split_cnt_cap, sizeof(unsigned) * (size_t)std::max<int64_t>(n + 1, 1));
+// The scheduling pass (one traversal of the arcs, two phases): probe totals of both plans, the
+// split's in-degree counts and work sums, the sortedness check (TC_DEV_UNSORTED in ctl), the list
+// of rows longer than TC_SCHED_FLAT (kept for split_build), and - with a model - every long row's
+// predicted cycles and class decision plus the predicted saving of the split.  Enqueued only:
+// the totals reach the host with the stream's next synchronisation (split_plan_read).
+int split_plan(trust_tc_ctx *c, const int64_t *beg, const int32_t *adj, int64_t n, int64_t m, cudaStream_t st,
+               const float *d_model, int warp_max, int cta_max, float promote_log2, int cta_warps, TcControl *ctl) {
+  const size_t nn = (size_t)std::max<int64_t>(n + 1, 1);
+  int rc = ensure((void **)&c->d_split_cnt, &c->split_cnt_cap, sizeof(unsigned) * nn);
   if (rc) return rc;
-  rc = ensure((void **)&c->d_split_plans, &c->split_plans_cap, 4 * sizeof(unsigned long long));
-  if (rc) return rc;
-  rc = ensure((void **)&c->d_split_wsum, &c->split_wsum_cap, sizeof(unsigned long long) * (size_t)(n + 1));
-  if (rc) return rc;
+  if ((rc = ensure((void **)&c->d_split_plans, &c->split_plans_cap, TC_PLAN_WORDS * sizeof(unsigned long long))))
+    return rc;
+  if ((rc = ensure((void **)&c->d_split_wsum, &c->split_wsum_cap, sizeof(unsigned long long) * nn))) return rc;
+  if ((rc = ensure((void **)&c->d_sched_long, &c->sched_long_cap, sizeof(int) * nn))) return rc;
+  if ((rc = ensure((void **)&c->d_split_pairs, &c->split_pairs_cap, sizeof(int2) * (size_t)std::max<int64_t>(m, 1))))
+    return rc;
+  if ((rc = ensure((void **)&c->d_split_ranks, &c->split_ranks_cap, sizeof(unsigned) * (size_t)std::max<int64_t>(m, 1))))
+    return rc;
   if (d_model) {
-    if ((rc = ensure((void **)&c->d_dec, &c->dec_cap, (size_t)std::max<int64_t>(n, 1)))) return rc;
-    if ((rc = ensure((void **)&c->d_pred, &c->pred_cap, sizeof(float) * (size_t)std::max<int64_t>(n, 1)))) return rc;
+    if ((rc = ensure((void **)&c->d_dec, &c->dec_cap, nn))) return rc;
+    if ((rc = ensure((void **)&c->d_pred, &c->pred_cap, sizeof(float) * nn))) return rc;
   }
   TC_CUDA_TRY(cudaMemsetAsync(c->d_split_cnt, 0, sizeof(unsigned) * (size_t)(n + 1), st));
   TC_CUDA_TRY(cudaMemsetAsync(c->d_split_wsum, 0, sizeof(unsigned long long) * (size_t)(n + 1), st));
-  TC_CUDA_TRY(cudaMemsetAsync(c->d_split_plans, 0, 4 * sizeof(unsigned long long), st));
-  float *sums = reinterpret_cast<float *>(c->d_split_plans + 2);
-  const int blocks = arc_blocks(n, c->num_sms);
-  if (d_model)
-    sched_kernel<true><<<blocks, 256, 0, st>>>(beg, adj, n, c->d_split_cnt, c->d_split_wsum, c->d_split_plans, d_model,
-                                               warp_max, cta_max, promote_log2, c->d_dec, c->d_pred, sums, d_features,
-                                               cta_warps);
-  else
-    sched_kernel<false><<<blocks, 256, 0, st>>>(beg, adj, n, c->d_split_cnt, c->d_split_wsum, c->d_split_plans,
-                                                nullptr, warp_max, cta_max, promote_log2, nullptr, nullptr, nullptr,
-                                                d_features, cta_warps);
+  TC_CUDA_TRY(cudaMemsetAsync(c->d_split_plans, 0, TC_PLAN_WORDS * sizeof(unsigned long long), st));
+  float *sums = reinterpret_cast<float *>(c->d_split_plans + PLAN_SAVED);
+  sched_short_kernel<<<arc_blocks(n, c->num_sms), 256, 0, st>>>(beg, adj, n, c->d_split_cnt, c->d_split_wsum,
+                                                                c->d_split_plans, c->d_sched_long, c->d_split_pairs,
+                                                                c->d_split_ranks, ctl);
   TC_CUDA_TRY(cudaGetLastError());
-  unsigned long long hp[4];
-  TC_CUDA_TRY(cudaMemcpyAsync(hp, c->d_split_plans, sizeof hp, cudaMemcpyDeviceToHost, st));
-  TC_CUDA_TRY(cudaStreamSynchronize(st));
-  plan->w_all = hp[0];
-  plan->w_min = hp[1];
-  float saved = 0.f;
-  memcpy(&saved, &hp[2], sizeof saved);
-  plan->saved_cycles = saved;
+  const int lb = c->num_sms * 8;
+  if (d_model)
+    sched_long_kernel<true><<<lb, 256, 0, st>>>(beg, adj, c->d_split_cnt, c->d_split_wsum, c->d_split_plans,
+                                                c->d_sched_long, d_model, warp_max, cta_max, promote_log2, c->d_dec,
+                                                c->d_pred, sums, cta_warps, c->d_split_pairs, c->d_split_ranks, ctl);
+  else
+    sched_long_kernel<false><<<lb, 256, 0, st>>>(beg, adj, c->d_split_cnt, c->d_split_wsum, c->d_split_plans,
+                                                 c->d_sched_long, nullptr, warp_max, cta_max, promote_log2, nullptr,
+                                                 nullptr, nullptr, cta_warps, c->d_split_pairs, c->d_split_ranks, ctl);
+  TC_CUDA_TRY(cudaGetLastError());
+  TC_CUDA_TRY(cudaMemcpyAsync(c->h_plans, c->d_split_plans, TC_PLAN_WORDS * sizeof(unsigned long long),
+                              cudaMemcpyDeviceToHost, st));
   return TRUST_TC_OK;
 }
 
-// Build the second pass's work rows (after split_plan): the in-list of every target, cut into
-// chunks (chunk_len) so one heavily targeted row spreads over many CTAs.
+void split_plan_read(const trust_tc_ctx *c, SchedPlan *plan) {
+  plan->w_all = c->h_plans[PLAN_W_ALL];
+  plan->w_min = c->h_plans[PLAN_W_MIN];
+  float saved = 0.f;
+  memcpy(&saved, &c->h_plans[PLAN_SAVED], sizeof saved);
+  plan->saved_cycles = saved;
+  plan->long_rows = (int64_t)c->h_plans[PLAN_NLONG];
+  plan->moved_arcs = (int64_t)c->h_plans[PLAN_NPAIRS];
+}
+
+// Build the second pass's work rows (after split_plan, whose long-row list it reuses): the
+// in-list of every target, cut into chunks so one heavily targeted row spreads over many CTAs.
 // Outputs live in the context.
 int split_build(trust_tc_ctx *c, const int64_t *beg, const int32_t *adj, int64_t n, int64_t m, cudaStream_t st,
                 SplitRows *out) {
@@ -439,8 +482,8 @@ int split_build(trust_tc_ctx *c, const int64_t *beg, const int32_t *adj, int64_t
   if ((rc = scan_exclusive_i64(c->d_split_cbase, c->d_split_cbase, n + 1, st, &nchunks))) return rc;
   if (nchunks > max_chunks) return TRUST_TC_E_DEVICE;
   // scatter the sources
-  TC_CUDA_TRY(cudaMemsetAsync(c->d_split_cnt, 0, sizeof(unsigned) * (size_t)(n + 1), st));
-  split_fill_kernel<<<arc_blocks(n, c->num_sms), 256, 0, st>>>(beg, adj, n, c->d_split_cnt, c->d_split_beg,
+  split_fill_kernel<<<arc_blocks(m, c->num_sms), 256, 0, st>>>(c->d_split_pairs, c->d_split_ranks,
+                                                               c->d_split_plans + PLAN_NPAIRS, c->d_split_beg,
                                                                c->d_split_adj);
   TC_CUDA_TRY(cudaGetLastError());
   chunk_fill_kernel<<<vb, 256, 0, st>>>(c->d_split_cbase, c->d_split_beg, n, total, nchunks, c->d_split_cbeg,
@@ -455,40 +498,97 @@ int split_build(trust_tc_ctx *c, const int64_t *beg, const int32_t *adj, int64_t
 }
 
 // ---- heaviest-first queue order ------------------------------------------------------------------
-__global__ void lpt_keys_kernel(const int *__restrict__ list, int count, const float *__restrict__ pred,
-                                unsigned long long *__restrict__ keys) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
-    const int v = list[i];
-    const float y = fminf(fmaxf(pred[v], 0.f), 63.9f);
-    const unsigned q = 65535u - (unsigned)(y * 1024.f);  // larger prediction sorts first
-    keys[i] = ((unsigned long long)q << 32) | (unsigned)v;
-  }
+// A counting sort of the warp, CTA and huge lists (adjacent in the list buffer, in that order) by
+// predicted cost, descending, in buckets of 1/8 log2 cycle.  The order inside a bucket is
+// arbitrary: a work queue only needs its long rows first.
+constexpr int TC_LPT_BUCKETS = 256;
+constexpr int TC_LPT_KEYS = 3 * TC_LPT_BUCKETS;  // (class, bucket)
+
+struct LptRange {
+  int lo, cta, huge, hi;  // list indices: [lo, cta) warp, [cta, huge) CTA, [huge, hi) huge
+};
+
+__device__ __forceinline__ int lpt_key(const LptRange &r, int i, float y) {
+  const int c = i < r.cta ? 0 : (i < r.huge ? 1 : 2);
+  const int q = (int)(fminf(fmaxf(y, 0.f), 31.99f) * 8.f);  // 0..255
+  return c * TC_LPT_BUCKETS + (TC_LPT_BUCKETS - 1 - q);     // larger prediction first
 }
 
-__global__ void lpt_store_kernel(const unsigned long long *__restrict__ keys, int count, int *__restrict__ list) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x)
-    list[i] = (int)(keys[i] & 0xffffffffu);
+__global__ void lpt_hist_kernel(const int *__restrict__ lists, LptRange r, const float *__restrict__ pred,
+                                unsigned *__restrict__ hist) {
+  __shared__ unsigned h[TC_LPT_KEYS];
+  for (int i = threadIdx.x; i < TC_LPT_KEYS; i += blockDim.x) h[i] = 0;
+  __syncthreads();
+  for (int i = r.lo + blockIdx.x * blockDim.x + threadIdx.x; i < r.hi; i += gridDim.x * blockDim.x)
+    atomicAdd(&h[lpt_key(r, i, pred[lists[i]])], 1u);
+  __syncthreads();
+  for (int i = threadIdx.x; i < TC_LPT_KEYS; i += blockDim.x)
+    if (h[i]) atomicAdd(hist + i, h[i]);
+}
+
+// Every CTA (256 threads) scans the histogram itself, then places its items through per-key
+// cursors (one atomic per key and warp).  out[] is indexed from r.lo.
+__global__ void __launch_bounds__(256) lpt_scatter_kernel(const int *__restrict__ lists, LptRange r,
+                                                          const float *__restrict__ pred,
+                                                          const unsigned *__restrict__ hist,
+                                                          unsigned *__restrict__ cursor, int *__restrict__ out) {
+  __shared__ unsigned base[TC_LPT_KEYS];
+  __shared__ unsigned wsum[8];
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  const int cls_start[3] = {0, r.cta - r.lo, r.huge - r.lo};
+  for (int c = 0; c < 3; ++c) {  // exclusive scan of class c's buckets, thread t owns bucket t
+    const unsigned x = hist[c * TC_LPT_BUCKETS + t];
+    unsigned incl = x;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned y = __shfl_up_sync(TC_FULL_MASK, incl, o);
+      if (lane >= o) incl += y;
+    }
+    if (lane == 31) wsum[w] = incl;
+    __syncthreads();
+    unsigned before = 0;
+    for (int k = 0; k < w; ++k) before += wsum[k];
+    base[c * TC_LPT_BUCKETS + t] = (unsigned)cls_start[c] + before + incl - x;
+    __syncthreads();
+  }
+  for (int i0 = r.lo + blockIdx.x * blockDim.x; i0 < r.hi; i0 += gridDim.x * blockDim.x) {
+    const int i = i0 + t;
+    int key = -1, v = 0;
+    if (i < r.hi) {
+      v = lists[i];
+      key = lpt_key(r, i, pred[v]);
+    }
+    const unsigned peers = __match_any_sync(TC_FULL_MASK, key);
+    const int leader = __ffs(peers) - 1;
+    unsigned at = 0;
+    if (key >= 0 && lane == leader) at = atomicAdd(cursor + key, (unsigned)__popc(peers));
+    at = __shfl_sync(TC_FULL_MASK, at, leader);
+    if (key >= 0) out[base[key] + at + __popc(peers & tc_lanemask_lt())] = v;
+  }
 }
 
 int lpt_sort(trust_tc_ctx *c, int *lists, const int *off, const int *counts, const float *pred, cudaStream_t st) {
-  const int classes[3] = {TC_CLASS_HUGE, TC_CLASS_CTA, TC_CLASS_WARP};
-  int64_t most = 0;
-  for (int k : classes) most = std::max<int64_t>(most, counts[k]);
-  if (most < 2) return TRUST_TC_OK;
-  int rc = ensure((void **)&c->d_sort, &c->sort_cap, sizeof(unsigned long long) * 2 * (size_t)most);
+  LptRange r;
+  r.lo = off[TC_CLASS_WARP];
+  r.cta = off[TC_CLASS_CTA];
+  r.huge = off[TC_CLASS_HUGE];
+  r.hi = off[TC_CLASS_HUGE] + counts[TC_CLASS_HUGE];
+  const int total = r.hi - r.lo;
+  if (total < 2) return TRUST_TC_OK;
+  // scratch: histogram and cursors (2 x TC_LPT_KEYS u32), then the sorted copy
+  const size_t bytes = sizeof(unsigned) * (2 * (size_t)TC_LPT_KEYS + (size_t)total);
+  int rc = ensure((void **)&c->d_sort, &c->sort_cap, bytes);
   if (rc) return rc;
-  const int shifts[2] = {32, 40};  // the 16-bit cost key only; the sort is stable
-  for (int k : classes) {
-    const int cnt = counts[k];
-    if (cnt < 2) continue;
-    const int blocks = std::max(1, std::min((cnt + 255) / 256, c->num_sms * 8));
-    lpt_keys_kernel<<<blocks, 256, 0, st>>>(lists + off[k], cnt, pred, c->d_sort);
-    TC_CUDA_TRY(cudaGetLastError());
-    rc = radix_sort_u64(c->d_sort, c->d_sort + most, cnt, shifts, 2, st);
-    if (rc) return rc;
-    lpt_store_kernel<<<blocks, 256, 0, st>>>(c->d_sort, cnt, lists + off[k]);
-    TC_CUDA_TRY(cudaGetLastError());
-  }
+  unsigned *hist = reinterpret_cast<unsigned *>(c->d_sort);
+  unsigned *cursor = hist + TC_LPT_KEYS;
+  int *out = reinterpret_cast<int *>(cursor + TC_LPT_KEYS);
+  TC_CUDA_TRY(cudaMemsetAsync(hist, 0, sizeof(unsigned) * 2 * TC_LPT_KEYS, st));
+  const int blocks = std::max(1, std::min((total + 255) / 256, c->num_sms * 2));
+  lpt_hist_kernel<<<blocks, 256, 0, st>>>(lists, r, pred, hist);
+  TC_CUDA_TRY(cudaGetLastError());
+  lpt_scatter_kernel<<<blocks, 256, 0, st>>>(lists, r, pred, hist, cursor, out);
+  TC_CUDA_TRY(cudaGetLastError());
+  TC_CUDA_TRY(cudaMemcpyAsync(lists + r.lo, out, sizeof(int) * (size_t)total, cudaMemcpyDeviceToDevice, st));
   return TRUST_TC_OK;
 }
 
