@@ -4,14 +4,18 @@ Workload (default): the Chung-Lu power-law graph with 3.8M vertices, degree expo
 expected degree 800, ~16.5M undirected edges, seed 2 — the synthetic stand-in for the reference's
 Cit-Patents example (generated on the GPU, GPU-preprocessed to an oriented int32 CSR with int64
 offsets).  A step is one counting call over the whole graph.  Metric: TEPS = m / t, printed by the
-reference as GTEPS (Without-graph-partition/mpi_main.cpp:124).
+reference as GTEPS (Without-graph-partition/mpi_main.cpp:124), for the library's default (learned)
+schedule, with the plain degree-threshold schedule (the reference's USE_WARP/USE_CTA split) and
+the tuned classes measured in the same run.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload NAME]
 
 Rank 0 prints one JSON line.  `value` times the device-resident call (validation, classification,
-counting); `e2e` times the same call through the C ABI with pinned host buffers (H2D copy and the
-result read inside the timed region); `roofline` relates the counting kernel's algorithmic bytes
-to the measured HBM copy bandwidth; `cpu_baseline` is the CPU forward-intersection counter.
+scheduling, counting); `e2e` times the same call through the C ABI with pinned host buffers (H2D
+copy and the result read inside the timed region); `roofline` relates the counting kernel's
+algorithmic bytes to the measured HBM copy bandwidth; `cpu_baseline` is the CPU
+forward-intersection counter; `gpu_launches` is the library's own launch counter over the timed
+region.
 """
 from __future__ import annotations
 
@@ -38,7 +42,7 @@ WORKLOADS = {
 }
 DEFAULT_WORKLOAD = "chung_lu_3.8m"
 L2_FLUSH_BYTES = 256 << 20  # > 126 MB L2; the default graph (~96 MB) fits in L2, so flush every step
-KERNELS_PER_CALL = 4        # check, classify histogram, classify scatter, count
+METRIC = "TEPS on 1 GB300: learned/autotuned vs plain TRUST schedule; % HBM roofline"
 
 
 def _peaks():
@@ -177,7 +181,6 @@ def cpu_baseline(beg_np, adj_np, budget_s: float = 12.0):
 
 
 def run_ours(args, ws, rank, local):
-    import numpy as np
     import torch
     import trust_gb300 as T
 
@@ -192,9 +195,10 @@ def run_ours(args, ws, rank, local):
     stream = torch.cuda.current_stream()
     ctx = T.Context(local)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device="cuda")
+    lib = T.load()
 
-    def call():
-        return T.count_csr(beg, adj, ctx=ctx, stream=stream.cuda_stream)
+    def call(schedule=T.SCHED_LEARNED):
+        return T.count_csr(beg, adj, ctx=ctx, stream=stream.cuda_stream, schedule=schedule)
 
     for _ in range(args.warmup):
         r = call()
@@ -204,6 +208,7 @@ def run_ours(args, ws, rank, local):
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
+    launches0 = lib.trust_tc_kernel_launches()
     with ClockSampler(local) as clk:
         for i in range(args.steps):
             flush.fill_(i)
@@ -211,6 +216,7 @@ def run_ours(args, ws, rank, local):
             res.append(call())
             ev[i][1].record(stream)
         torch.cuda.synchronize()
+    launches = lib.trust_tc_kernel_launches() - launches0
     if dist:
         dist.barrier()
     clocks = clk.summary()
@@ -224,6 +230,25 @@ def run_ours(args, ws, rank, local):
     count_s = statistics.median(r.count_seconds for r in res)
     kernel_s = statistics.median(r.kernel_seconds for r in res)
     wedges = res[0].wedges
+
+    # the same call under the other schedules (same flush discipline), for the learned-vs-plain ratio
+    sched = {"learned": {"gteps": m / (statistics.median(step_ms) * 1e-3) / 1e9,
+                         "ms": statistics.median(step_ms), "direction_split": res[0].direction_split,
+                         "predicted_split_saving_ms": res[0].split_saving_ms}}
+    for name, code in (("tuned", T.SCHED_TUNED), ("plain", T.SCHED_PLAIN)):
+        call(code)
+        ms = []
+        for i in range(max(5, args.steps // 10)):
+            flush.fill_(i)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            r3 = call(code)
+            b.record(stream)
+            torch.cuda.synchronize()
+            ms.append(a.elapsed_time(b))
+            ok = ok and r3.triangles == expect_count
+        sched[name] = {"gteps": m / (statistics.median(ms) * 1e-3) / 1e9, "ms": statistics.median(ms),
+                       "count_kernel_ms": r3.count_seconds * 1e3}
 
     # end to end through the C ABI: pinned host buffers, H2D + count + result read inside the region
     hb = beg.cpu().pin_memory()
@@ -250,7 +275,7 @@ def run_ours(args, ws, rank, local):
     algo_bytes = 24 * m + 8 * (n + 1) + 4 * wedges
     achieved = algo_bytes / count_s / 1e9
     line = {
-        "metric": "TEPS = undirected edges / counting time (reference formula), plain degree-threshold schedule",
+        "metric": METRIC,
         "value": ws * m * args.steps / (total_ms * 1e-3) / 1e9,
         "unit": "GTEPS",
         "n_gpus": ws,
@@ -263,15 +288,18 @@ def run_ours(args, ws, rank, local):
         "dtype": "int32",
         "data": "synthetic (seeded generator on the GPU, GPU-preprocessed oriented CSR); no dataset download",
         "config": {"workload": w["desc"], "vertices": n, "edges": m, "wedges": wedges, "triangles": expect_count,
-                   "schedule": "plain", "class_sizes": res[0].class_sizes, "parallelism": f"replicas x{ws}",
+                   "schedule": "learned (library default)", "class_sizes": res[0].class_sizes,
+                   "parallelism": f"replicas x{ws}",
                    "l2": f"{L2_FLUSH_BYTES >> 20} MiB buffer written before every timed step (graph "
                          f"{(8 * (n + 1) + 4 * m) / 1e6:.0f} MB fits in L2)"},
+        "schedules": sched,
+        "learned_vs_plain": sched["learned"]["gteps"] / sched["plain"]["gteps"],
         "counts_consistent": ok,
         "kernel_ms": kernel_s * 1e3,
         "count_kernel_ms": count_s * 1e3,
-        "gpu_launches": KERNELS_PER_CALL * args.steps,
+        "gpu_launches": int(launches),
         "e2e": {"value": m / (e2e_mean * 1e-3) / 1e9, "unit": "GTEPS",
-                "h2d_bytes_per_step": 8 * (n + 1) + 4 * m, "d2h_bytes_per_step": int(T.load().trust_tc_readback_bytes()),
+                "h2d_bytes_per_step": 8 * (n + 1) + 4 * m, "d2h_bytes_per_step": int(lib.trust_tc_readback_bytes()),
                 "ms_per_step": e2e_mean},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": _traffic(args.workload), "peak_source": peak_src,
@@ -318,11 +346,11 @@ def run_reference(args, ws, rank, local):
     value = tot_arcs / tot_t / 1e9
     line = {
         "impl": "reference",
-        "metric": "TEPS = undirected edges / counting time (reference formula), plain degree-threshold schedule",
+        "metric": METRIC,
         "value": value, "unit": "GTEPS", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": tot_t / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded generator, CPU oracle pipeline)",
-        "config": {"workload": w["desc"], "vertices": n, "edges": m, "schedule": "plain"},
+        "config": {"workload": w["desc"], "vertices": n, "edges": m, "schedule": "n/a: CPU forward intersection"},
         "cpu_baseline": {"value": value, "unit": "GTEPS", "cores": threads, "kind": "port",
                          "sample": f"one of {slices} vertex slices per step (~{m // slices} arcs), forward "
                                    f"intersection over presorted rows, {threads} threads"},

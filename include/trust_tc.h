@@ -51,9 +51,12 @@ enum { TRUST_TC_HOST = 0, TRUST_TC_DEVICE = 1 };
 enum {
   TRUST_TC_SCHED_PLAIN = 0,   /* the reference's split: one warp per vertex for out-degree 2..100,
                                  one CTA above (USE_WARP / USE_CTA, Without-graph-partition/TC.cu:19-20) */
-  TRUST_TC_SCHED_LEARNED = 1, /* TUNED classes, then a per-vertex cost model promotes heavy vertices
-                                 to CTA granularity and orders the CTA and warp queues by cost       */
-  TRUST_TC_SCHED_TUNED = 2    /* sub-warp degree classes (4, 8, 16, 32 lanes), warp, CTA (default)   */
+  TRUST_TC_SCHED_LEARNED = 1, /* (default) TUNED classes; on graphs of at least 2^23 arcs with skewed
+                                 rows a scheduling pass runs a per-vertex cost model that promotes
+                                 heavy vertices to CTA granularity, orders the warp, CTA and huge
+                                 queues by predicted cost and decides the direction split from its
+                                 predicted saving                                                    */
+  TRUST_TC_SCHED_TUNED = 2    /* sub-warp degree classes (4, 8, 16, 32 lanes), warp, CTA             */
 };
 
 /* validation level for device-resident input (host input is always fully validated) */
@@ -105,6 +108,8 @@ const char *trust_tc_last_cuda_error(void);
 const char *trust_tc_version(void);
 /* bytes read back from the device per counting call (status words and the count) */
 size_t trust_tc_readback_bytes(void);
+/* kernels this library has launched since it was loaded (all threads and contexts) */
+uint64_t trust_tc_kernel_launches(void);
 
 /* A context owns device scratch (work queues, class lists, spill tables, staging copies of
  * host input) and reuses it across calls.  Not thread-safe; separate contexts are independent.

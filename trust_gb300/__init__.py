@@ -64,7 +64,7 @@ def _result(r: _lib.Result) -> CountResult:
 
 
 def _opts(threads=0, blocks=0, chunk=0, ptr_kind=HOST, validate=VALIDATE_FULL, warp_max=0, block_max=0,
-          stream=None, device=-1, schedule=SCHED_TUNED) -> _lib.Opts:
+          stream=None, device=-1, schedule=SCHED_LEARNED) -> _lib.Opts:
     o = _lib.Opts()
     load().trust_tc_opts_init(C.byref(o))
     o.device = device
@@ -111,7 +111,7 @@ def _is_torch_cuda(x) -> bool:
 
 
 def count_csr(beg, adj, *, ctx: Context | None = None, threads=0, blocks=0, chunk=0, stream=None,
-              validate=VALIDATE_FULL, warp_max=0, block_max=0, schedule=SCHED_TUNED,
+              validate=VALIDATE_FULL, warp_max=0, block_max=0, schedule=SCHED_LEARNED,
               cycles=None, direction_split=-1, model=None) -> CountResult:
     """Count over a CSR held in numpy arrays (host) or contiguous torch CUDA tensors (device).
 

@@ -64,6 +64,7 @@ SIGNATURES = {
     "trust_tc_last_cuda_error": (C.c_char_p, []),
     "trust_tc_version": (C.c_char_p, []),
     "trust_tc_readback_bytes": (C.c_size_t, []),
+    "trust_tc_kernel_launches": (C.c_uint64, []),
     "trust_tc_ctx_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int]),
     "trust_tc_ctx_destroy": (C.c_int, [_P]),
     "trust_tc_validate_csr": (C.c_int, [_P, _P, C.c_int64, C.c_int64, _I64P]),

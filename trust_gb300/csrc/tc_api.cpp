@@ -14,6 +14,7 @@
 #include <sys/stat.h>
 
 #include <algorithm>
+#include <atomic>
 #include <string>
 
 #include "tc_count.h"
@@ -23,6 +24,9 @@
 namespace tc {
 
 static thread_local char g_cuda_err[256] = "";
+static std::atomic<uint64_t> g_kernel_launches{0};
+
+void note_launch() { g_kernel_launches.fetch_add(1, std::memory_order_relaxed); }
 
 int cuda_status(cudaError_t e) {
   if (e == cudaSuccess) return TRUST_TC_OK;
@@ -400,7 +404,7 @@ void trust_tc_opts_init(trust_tc_opts *o) {
   memset(o, 0, sizeof *o);
   o->device = -1;
   o->ptr_kind = TRUST_TC_HOST;
-  o->schedule = TRUST_TC_SCHED_TUNED;
+  o->schedule = TRUST_TC_SCHED_LEARNED;
   o->validate = TRUST_TC_VALIDATE_FULL;
   o->direction_split = -1;
 }
@@ -428,6 +432,8 @@ const char *trust_tc_last_cuda_error(void) { return g_cuda_err; }
 const char *trust_tc_version(void) { return "trust-gb300 0.1 (sm_103a)"; }
 
 size_t trust_tc_readback_bytes(void) { return 2 * sizeof(TcControl); }
+
+uint64_t trust_tc_kernel_launches(void) { return g_kernel_launches.load(std::memory_order_relaxed); }
 
 int trust_tc_ctx_create(trust_tc_ctx **out, int device) {
   if (!out) return TRUST_TC_E_ARG;

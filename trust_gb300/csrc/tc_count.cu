@@ -698,6 +698,7 @@ int launch_check(const int64_t *beg, const int32_t *adj, int64_t rows, int64_t m
   int blocks = (int)std::min<int64_t>((work + 255) / 256, (int64_t)num_sms * 8);
   blocks = std::max(blocks, 1);
   check_kernel<<<blocks, 256, 0, st>>>(beg, adj, rows, m, id_bound, check_ids, ctl);
+  TC_NOTE_LAUNCH();
   TC_CUDA_TRY(cudaGetLastError());
   return TRUST_TC_OK;
 }
@@ -714,6 +715,7 @@ int launch_classify(int pass, const int64_t *begA, const int64_t *begB, int64_t 
   else
     class_kernel<1><<<blocks, 256, 0, st>>>(begA, begB, rows, min_deg, warp_max, cta_max, plain, rowmap, dec, ctl,
                                             lists, off);
+  TC_NOTE_LAUNCH();
   TC_CUDA_TRY(cudaGetLastError());
   return TRUST_TC_OK;
 }
@@ -776,6 +778,7 @@ static void launch_one(const CountArgs &a, int blocks, int threads, size_t smem_
     count_kernel<SAME, true, MAXT, MINB><<<blocks, threads, smem_bytes, st>>>(a);
   else
     count_kernel<SAME, false, MAXT, MINB><<<blocks, threads, smem_bytes, st>>>(a);
+  TC_NOTE_LAUNCH();
 }
 
 int launch_count(bool same, const CountArgs &a, int blocks, int threads, size_t smem_bytes,

@@ -110,7 +110,10 @@ int trust_tc_gen_rmat_device(trust_tc_ctx *ctx, int scale, int64_t npairs, doubl
   const double s32 = 4294967296.0;
   unsigned ta = (unsigned)std::min(a * s32, s32 - 1), tab = (unsigned)std::min((a + b) * s32, s32 - 1),
            tabc = (unsigned)std::min((a + b + c) * s32, s32 - 1);
-  if (npairs) rmat_kernel<<<gen_grid(npairs), 256>>>(scale, npairs, ta, tab, tabc, gen_key(seed), d_pairs);
+  if (npairs) {
+    rmat_kernel<<<gen_grid(npairs), 256>>>(scale, npairs, ta, tab, tabc, gen_key(seed), d_pairs);
+    TC_NOTE_LAUNCH();
+  }
   TC_CUDA_TRY(cudaGetLastError());
   TC_CUDA_TRY(cudaDeviceSynchronize());
   return TRUST_TC_OK;
@@ -126,6 +129,7 @@ int trust_tc_gen_chung_lu_device(trust_tc_ctx *ctx, int64_t n, double gamma, dou
   trust_tc_chung_lu_table(n, gamma, w_max, target_edges, cdf.data());
   uint64_t *d_cdf = nullptr;
   TC_CUDA_TRY(cudaMalloc(&d_cdf, sizeof(uint64_t) * (size_t)n));
+  TC_NOTE_LAUNCH();
   cudaError_t e = cudaMemcpy(d_cdf, cdf.data(), sizeof(uint64_t) * (size_t)n, cudaMemcpyHostToDevice);
   if (e == cudaSuccess && npairs) {
     weighted_kernel<<<gen_grid(npairs), 256>>>((const u64 *)d_cdf, n, npairs, gen_key(seed), d_pairs);
@@ -139,6 +143,7 @@ int trust_tc_gen_chung_lu_device(trust_tc_ctx *ctx, int64_t n, double gamma, dou
 
 int trust_tc_gen_er_device(trust_tc_ctx *ctx, int64_t n, int64_t npairs, uint64_t seed, int32_t *d_pairs) {
   if (n < 1 || n >= ((int64_t)1 << 31) || npairs < 0 || (npairs && !d_pairs)) return TRUST_TC_E_ARG;
+TC_NOTE_LAUNCH();
   if (ctx) TC_CUDA_TRY(cudaSetDevice(ctx->device));
   if (npairs) er_kernel<<<gen_grid(npairs), 256>>>(n, npairs, gen_key(seed), d_pairs);
   TC_CUDA_TRY(cudaGetLastError());

@@ -182,6 +182,7 @@ int trust_tc_model_grad(const float *d_x, const float *d_y, int64_t n, const flo
   if (e == cudaSuccess) e = cudaMemset(dG, 0, sizeof(float) * (TC_MODEL_FLOATS + 1));
   if (e == cudaSuccess) {
     mlp_grad_kernel<<<(unsigned)((n + 127) / 128), 128>>>(dP, d_x, d_y, n, dG, dL);
+    TC_NOTE_LAUNCH();
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) e = cudaMemcpy(grad, dG, sizeof(float) * TC_MODEL_FLOATS, cudaMemcpyDeviceToHost);
@@ -235,13 +236,16 @@ int trust_tc_model_train(const float *d_x, const float *d_y, int64_t n, int epoc
       e = cudaMemsetAsync(dG, 0, sizeof(float) * nf);
       if (e != cudaSuccess) break;
       mlp_grad_kernel<<<(unsigned)((cnt + 127) / 128), 128>>>(dP, d_x + off * TC_FEATURES, d_y + off, cnt, dG, nullptr);
+      TC_NOTE_LAUNCH();
       adam_kernel<<<(TC_MODEL_FLOATS + 255) / 256, 256>>>(dP, dG, dM, dV, ++step, lr, 0.9f, 0.999f, 1e-8f);
+      TC_NOTE_LAUNCH();
       e = cudaGetLastError();
     }
   }
   if (e == cudaSuccess) e = cudaMemset(dG, 0, sizeof(float) * (nf + 1));
   if (e == cudaSuccess) {
     mlp_grad_kernel<<<(unsigned)((n + 127) / 128), 128>>>(dP, d_x, d_y, n, dG, dL);
+    TC_NOTE_LAUNCH();
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) e = cudaMemcpy(model, dP, sizeof(float) * nf, cudaMemcpyDeviceToHost);
@@ -260,6 +264,7 @@ int trust_tc_model_predict(const float *d_x, int64_t n, const float *model, floa
   cudaError_t e = cudaMemcpy(dP, model, sizeof(float) * TC_MODEL_FLOATS, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) {
     predict_kernel<<<(unsigned)((n + 127) / 128), 128>>>(dP, d_x, n, d_out);
+    TC_NOTE_LAUNCH();
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) e = cudaDeviceSynchronize();

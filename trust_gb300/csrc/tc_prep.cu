@@ -101,11 +101,13 @@ static int scan_exclusive(const T *in, T *out, int64_t n, cudaStream_t st, T *to
   if (nb > 1) {
     TC_CUDA_TRY(cudaMallocAsync((void **)&sums, sizeof(T) * nb, st));
     scan_reduce_kernel<T><<<(unsigned)nb, RS_THREADS, 0, st>>>(in, n, sums);
+    TC_NOTE_LAUNCH();
     TC_CUDA_TRY(cudaGetLastError());
     int rc = scan_exclusive<T>(sums, sums, nb, st, (T *)nullptr);
     if (rc) return rc;
   }
   scan_down_kernel<T><<<(unsigned)nb, RS_THREADS, 0, st>>>(in, out, n, sums);
+  TC_NOTE_LAUNCH();
   TC_CUDA_TRY(cudaGetLastError());
   if (sums) TC_CUDA_TRY(cudaFreeAsync(sums, st));
   if (total_out) {
@@ -188,10 +190,12 @@ static int radix_sort(u64 *keys, u64 *tmp, int64_t n, const std::vector<int> &sh
   u64 *src = keys, *dst = tmp;
   for (int sh : shifts) {
     rs_hist_kernel<<<nb, RS_THREADS, 0, st>>>(src, n, sh, counts, nb);
+    TC_NOTE_LAUNCH();
     TC_CUDA_TRY(cudaGetLastError());
     int rc = scan_exclusive<u32>(counts, counts, 256 * (int64_t)nb, st, (u32 *)nullptr);
     if (rc) return rc;
     rs_scatter_kernel<<<nb, RS_THREADS, 0, st>>>(src, dst, n, sh, counts, nb);
+    TC_NOTE_LAUNCH();
     TC_CUDA_TRY(cudaGetLastError());
     std::swap(src, dst);
   }
@@ -348,23 +352,28 @@ int build_csr_device(const int32_t *d_pairs, int64_t np, int64_t id_bound, int64
   const int idb = bits_for(id_bound);  // covers the invalid marker id_bound
   // 1. canonical (min,max) keys, sorted; invalid pairs sort last
   canon_kernel<<<grid_for(np), 256, 0, st>>>(d_pairs, np, id_bound, keys);
+  TC_NOTE_LAUNCH();
   std::vector<int> sh;
   push_digits(sh, 0, bits_for(id_bound - 1));
   push_digits(sh, 32, idb);
   if ((rc = radix_sort(keys, tmp, np, sh, st))) return rc;
   // 2. unique
   unique_flags_kernel<<<grid_for(np), 256, 0, st>>>(keys, np, id_bound, flags);
+  TC_NOTE_LAUNCH();
   u32 nu32 = 0;
   if ((rc = scan_exclusive<u32>(flags, pos, np, st, &nu32))) return rc;
   const int64_t nu = nu32;
   u64 *e = tmp;  // unique edges live in tmp from here on
   compact_kernel<<<grid_for(np), 256, 0, st>>>(keys, flags, pos, np, e);
+  TC_NOTE_LAUNCH();
   // 3. degrees and compacted ids (vertices without edges dropped)
   u32 *deg, *cid;
   if ((rc = B.get(&deg, id_bound)) || (rc = B.get(&cid, id_bound))) return rc;
   TC_CUDA_TRY(cudaMemsetAsync(deg, 0, sizeof(u32) * id_bound, st));
   degree_kernel<<<grid_for(nu), 256, 0, st>>>(e, nu, deg);
+  TC_NOTE_LAUNCH();
   present_kernel<<<grid_for(id_bound), 256, 0, st>>>(deg, id_bound, cid);
+  TC_NOTE_LAUNCH();
   u32 n32 = 0;
   if ((rc = scan_exclusive<u32>(cid, cid, id_bound, st, &n32))) return rc;
   const int64_t n = n32;
@@ -373,8 +382,10 @@ int build_csr_device(const int32_t *d_pairs, int64_t np, int64_t id_bound, int64
   u32 *vpos, *od, *dmax;
   if ((rc = B.get(&vkeys, n)) || (rc = B.get(&vtmp, n)) || (rc = B.get(&vpos, n)) || (rc = B.get(&od, n)) || (rc = B.get(&dmax, 1))) return rc;
   vkey_kernel<<<grid_for(id_bound), 256, 0, st>>>(deg, cid, id_bound, vkeys);
+  TC_NOTE_LAUNCH();
   TC_CUDA_TRY(cudaMemsetAsync(dmax, 0, sizeof(u32), st));
   max_kernel<<<grid_for(id_bound), 256, 0, st>>>(deg, id_bound, dmax);
+  TC_NOTE_LAUNCH();
   u32 hdmax = 0;
   TC_CUDA_TRY(cudaMemcpyAsync(&hdmax, dmax, sizeof(u32), cudaMemcpyDeviceToHost, st));
   TC_CUDA_TRY(cudaStreamSynchronize(st));
@@ -383,22 +394,28 @@ int build_csr_device(const int32_t *d_pairs, int64_t np, int64_t id_bound, int64
   push_digits(sh, 32, bits_for(hdmax));
   if ((rc = radix_sort(vkeys, vtmp, n, sh, st))) return rc;
   position_kernel<<<grid_for(n), 256, 0, st>>>(vkeys, n, vpos);
+  TC_NOTE_LAUNCH();
   // 5. orient each edge from the earlier to the later vertex of that order
   TC_CUDA_TRY(cudaMemsetAsync(od, 0, sizeof(u32) * n, st));
   orient_kernel<<<grid_for(nu), 256, 0, st>>>(e, nu, cid, vpos, od);
+  TC_NOTE_LAUNCH();
   // 6. renumber: out-degree descending, ties by compacted id
   TC_CUDA_TRY(cudaMemsetAsync(dmax, 0, sizeof(u32), st));
   max_kernel<<<grid_for(n), 256, 0, st>>>(od, n, dmax);
+  TC_NOTE_LAUNCH();
   u32 hodmax = 0;
   TC_CUDA_TRY(cudaMemcpyAsync(&hodmax, dmax, sizeof(u32), cudaMemcpyDeviceToHost, st));
   TC_CUDA_TRY(cudaStreamSynchronize(st));
   renumber_key_kernel<<<grid_for(n), 256, 0, st>>>(od, n, hodmax, vkeys);
+  TC_NOTE_LAUNCH();
   sh.clear();
   push_digits(sh, 0, bits_for(std::max<int64_t>(n - 1, 1)));
   push_digits(sh, 32, bits_for(hodmax));
   if ((rc = radix_sort(vkeys, vtmp, n, sh, st))) return rc;
   position_kernel<<<grid_for(n), 256, 0, st>>>(vkeys, n, vpos);  // vpos = new id of compacted id
   relabel_kernel<<<grid_for(nu), 256, 0, st>>>(e, nu, vpos);
+  TC_NOTE_LAUNCH();
+  TC_NOTE_LAUNCH();
   // 7. sort arcs by (source, target) and emit the CSR
   sh.clear();
   push_digits(sh, 0, bits_for(std::max<int64_t>(n - 1, 1)));
@@ -419,8 +436,10 @@ int build_csr_device(const int32_t *d_pairs, int64_t np, int64_t id_bound, int64
     TC_CUDA_TRY(cudaStreamSynchronize(st));
     last_src = (int64_t)(last >> 32);
     csr_kernel<<<grid_for(nu), 256, 0, st>>>(e, nu, n, beg, adj);
+    TC_NOTE_LAUNCH();
   }
   csr_tail_kernel<<<grid_for(n + 1 - (last_src + 1)), 256, 0, st>>>(last_src + 1, n, nu, beg);
+  TC_NOTE_LAUNCH();
   cudaError_t le = cudaGetLastError();
   cudaError_t se = cudaStreamSynchronize(st);
   if (le != cudaSuccess || se != cudaSuccess) {

@@ -429,6 +429,7 @@ int split_plan(trust_tc_ctx *c, const int64_t *beg, const int32_t *adj, int64_t 
   sched_short_kernel<<<arc_blocks(n, c->num_sms), 256, 0, st>>>(beg, adj, n, c->d_split_cnt, c->d_split_wsum,
                                                                 c->d_split_plans, c->d_sched_long, c->d_split_pairs,
                                                                 c->d_split_ranks, ctl);
+  TC_NOTE_LAUNCH();
   TC_CUDA_TRY(cudaGetLastError());
   const int lb = c->num_sms * 8;
   if (d_model)
@@ -439,6 +440,7 @@ int split_plan(trust_tc_ctx *c, const int64_t *beg, const int32_t *adj, int64_t 
     sched_long_kernel<false><<<lb, 256, 0, st>>>(beg, adj, c->d_split_cnt, c->d_split_wsum, c->d_split_plans,
                                                  c->d_sched_long, nullptr, warp_max, cta_max, promote_log2, nullptr,
                                                  nullptr, nullptr, cta_warps, c->d_split_pairs, c->d_split_ranks, ctl);
+  TC_NOTE_LAUNCH();
   TC_CUDA_TRY(cudaGetLastError());
   TC_CUDA_TRY(cudaMemcpyAsync(c->h_plans, c->d_split_plans, TC_PLAN_WORDS * sizeof(unsigned long long),
                               cudaMemcpyDeviceToHost, st));
@@ -471,12 +473,14 @@ int split_build(trust_tc_ctx *c, const int64_t *beg, const int32_t *adj, int64_t
   const int vb = arc_blocks(n + 1, c->num_sms);
   // in-list offsets: exclusive scan of the in-degrees (entry n is 0)
   u32_to_i64_kernel<<<vb, 256, 0, st>>>(c->d_split_cnt, c->d_split_beg, n + 1);
+  TC_NOTE_LAUNCH();
   TC_CUDA_TRY(cudaGetLastError());
   int64_t total = 0;
   if ((rc = scan_exclusive_i64(c->d_split_beg, c->d_split_beg, n + 1, st, &total))) return rc;
   if (total > m) return TRUST_TC_E_DEVICE;
   // chunk bases
   chunk_count_kernel<<<vb, 256, 0, st>>>(beg, c->d_split_cnt, c->d_split_wsum, c->d_split_cbase, n);
+  TC_NOTE_LAUNCH();
   TC_CUDA_TRY(cudaGetLastError());
   int64_t nchunks = 0;
   if ((rc = scan_exclusive_i64(c->d_split_cbase, c->d_split_cbase, n + 1, st, &nchunks))) return rc;
@@ -485,9 +489,11 @@ int split_build(trust_tc_ctx *c, const int64_t *beg, const int32_t *adj, int64_t
   split_fill_kernel<<<arc_blocks(m, c->num_sms), 256, 0, st>>>(c->d_split_pairs, c->d_split_ranks,
                                                                c->d_split_plans + PLAN_NPAIRS, c->d_split_beg,
                                                                c->d_split_adj);
+  TC_NOTE_LAUNCH();
   TC_CUDA_TRY(cudaGetLastError());
   chunk_fill_kernel<<<vb, 256, 0, st>>>(c->d_split_cbase, c->d_split_beg, n, total, nchunks, c->d_split_cbeg,
                                         c->d_split_rowmap);
+  TC_NOTE_LAUNCH();
   TC_CUDA_TRY(cudaGetLastError());
   out->beg = c->d_split_cbeg;
   out->adj = c->d_split_adj;
@@ -585,8 +591,10 @@ int lpt_sort(trust_tc_ctx *c, int *lists, const int *off, const int *counts, con
   TC_CUDA_TRY(cudaMemsetAsync(hist, 0, sizeof(unsigned) * 2 * TC_LPT_KEYS, st));
   const int blocks = std::max(1, std::min((total + 255) / 256, c->num_sms * 2));
   lpt_hist_kernel<<<blocks, 256, 0, st>>>(lists, r, pred, hist);
+  TC_NOTE_LAUNCH();
   TC_CUDA_TRY(cudaGetLastError());
   lpt_scatter_kernel<<<blocks, 256, 0, st>>>(lists, r, pred, hist, cursor, out);
+  TC_NOTE_LAUNCH();
   TC_CUDA_TRY(cudaGetLastError());
   TC_CUDA_TRY(cudaMemcpyAsync(lists + r.lo, out, sizeof(int) * (size_t)total, cudaMemcpyDeviceToDevice, st));
   return TRUST_TC_OK;
@@ -632,6 +640,7 @@ int vertex_features(trust_tc_ctx *c, const int64_t *beg, const int32_t *adj, int
                     float *d_features, cudaStream_t st) {
   const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((n * 32 + 255) / 256, (int64_t)c->num_sms * 16));
   vertex_features_kernel<<<blocks, 256, 0, st>>>(beg, adj, n, warp_max, cta_max, d_features);
+  TC_NOTE_LAUNCH();
   TC_CUDA_TRY(cudaGetLastError());
   return TRUST_TC_OK;
 }
