@@ -181,6 +181,14 @@ int trust_tc_partition_folder(const char *folder, const int64_t *begin, const in
 int trust_tc_build_csr_device(trust_tc_ctx *ctx, const int32_t *d_pairs, int64_t npairs,
                               int64_t id_bound, int64_t **d_begin, int32_t **d_adj, int64_t *n,
                               int64_t *m);
+/* The same for a batch: pairs of many graphs in one array, graph g owning original ids
+ * [graph_vbeg[g], graph_vbeg[g+1]) (host array of num_graphs+1 entries, graph_vbeg[0] = 0).  New
+ * ids keep the original order (no out-degree renumbering), so every graph stays a contiguous
+ * range of rows; graph_vbeg_out (host, num_graphs+1) receives those ranges.  The result is the
+ * input of trust_tc_batch_create.  No counterpart in the reference (one graph per run). */
+int trust_tc_build_batch_device(trust_tc_ctx *ctx, const int32_t *d_pairs, int64_t npairs,
+                                const int64_t *graph_vbeg, int64_t num_graphs, int64_t **d_begin,
+                                int32_t **d_adj, int64_t *n, int64_t *m, int64_t *graph_vbeg_out);
 void trust_tc_free_device(void *p);
 /* Copy `bytes` between any two buffers the CUDA runtime can address (cudaMemcpyDefault); lets a
  * caller that owns memory through another allocator take over library-allocated outputs. */
@@ -195,6 +203,10 @@ int trust_tc_gen_rmat_device(trust_tc_ctx *ctx, int scale, int64_t npairs, doubl
 int trust_tc_gen_chung_lu_device(trust_tc_ctx *ctx, int64_t n, double gamma, double w_max,
                                  int64_t target_edges, int64_t npairs, uint64_t seed,
                                  int32_t *d_pairs);
+/* Barabasi-Albert preferential attachment: n vertices, d edges each (n*d pairs; vertex 0's d
+ * pairs are self loops, the seed graph), by the endpoint-copy method (Batagelj & Brandes 2005,
+ * per edge as in Sanders & Schulz 2016). */
+int trust_tc_gen_ba_device(trust_tc_ctx *ctx, int64_t n, int d, uint64_t seed, int32_t *d_pairs);
 /* The Chung-Lu cumulative endpoint table used by trust_tc_gen_chung_lu_device (host, n entries,
  * scaled to 2^63).  Returns i0. */
 double trust_tc_chung_lu_table(int64_t n, double gamma, double w_max, int64_t target_edges, uint64_t *cdf);

@@ -56,6 +56,8 @@ def _declare(lib):
     lib.orc_gen_weighted.argtypes = [_P, C.c_int64, C.c_int64, C.c_uint64, _P]
     lib.orc_gen_er.restype = None
     lib.orc_gen_er.argtypes = [C.c_int64, C.c_int64, C.c_uint64, _P]
+    lib.orc_gen_ba.restype = None
+    lib.orc_gen_ba.argtypes = [C.c_int64, C.c_int, C.c_uint64, _P]
     lib.orc_chung_lu_cdf.restype = C.c_double
     lib.orc_chung_lu_cdf.argtypes = [C.c_int64, C.c_double, C.c_double, C.c_int64, _P]
     lib.free.restype = None
@@ -202,6 +204,13 @@ def gen_weighted(cdf: np.ndarray, npairs: int, seed: int) -> np.ndarray:
 def gen_er(n: int, npairs: int, seed: int) -> np.ndarray:
     out = np.zeros((npairs, 2), dtype=np.int32)
     load().orc_gen_er(n, npairs, seed, _p(out))
+    return out
+
+
+def gen_ba(n: int, d: int, seed: int) -> np.ndarray:
+    """Barabasi-Albert pairs, d per vertex (vertex 0's are self loops): tc_oracle.c orc_gen_ba."""
+    out = np.zeros((n * d, 2), dtype=np.int32)
+    load().orc_gen_ba(n, d, seed, _p(out))
     return out
 
 

@@ -535,6 +535,29 @@ void orc_gen_er(i64 n, i64 np, u64 seed, i32 *out) {
   }
 }
 
+/* Barabasi-Albert graph with d edges per vertex: n*d pairs (v, target), vertex 0's d pairs are
+ * self loops.  The endpoint-copy method of Batagelj & Brandes (2005) in its per-edge form
+ * (Sanders & Schulz 2016): edge e of vertex v = e/d >= 1 draws r uniformly in [0, 2 v d); an
+ * even r names the source (r/2)/d, an odd r the target of edge (r-1)/2, resolved the same way.
+ * Restated here so the generator in trust_gb300/csrc/tc_gen.cu can be checked bit for bit. */
+static u64 ba_target(u64 key, u64 e, u64 d) {
+  for (;;) {
+    u64 v = e / d;
+    if (v == 0) return 0;
+    u64 r = (u64)(((unsigned __int128)draw(key, e, 0) * (2 * v * d)) >> 64);
+    if ((r & 1) == 0) return (r >> 1) / d;
+    e = r >> 1;
+  }
+}
+
+void orc_gen_ba(i64 n, int d, u64 seed, i32 *out) {
+  u64 key = orc_gen_key(seed);
+  for (i64 e = 0; e < n * (i64)d; ++e) {
+    out[2 * e] = (i32)(e / d);
+    out[2 * e + 1] = (i32)ba_target(key, (u64)e, (u64)d);
+  }
+}
+
 /* Chung-Lu expected degrees w_i = w_max * (1 + i/i0)^(-1/(gamma-1)), i0 chosen by bisection so
  * that the integral approximation of sum w equals 2*target_edges; cdf[i] = floor(2^63 * prefix_i /
  * total), cdf[n-1] = 2^63.  Returns i0. */

@@ -86,6 +86,10 @@ SIGNATURES = {
                                                C.c_uint64, _P]),
     "trust_tc_chung_lu_table": (C.c_double, [C.c_int64, C.c_double, C.c_double, C.c_int64, _P]),
     "trust_tc_gen_er_device": (C.c_int, [_P, C.c_int64, C.c_int64, C.c_uint64, _P]),
+    "trust_tc_gen_ba_device": (C.c_int, [_P, C.c_int64, C.c_int, C.c_uint64, _P]),
+    "trust_tc_build_batch_device": (C.c_int, [_P, _P, C.c_int64, _I64P, C.c_int64, C.POINTER(C.c_void_p),
+                                              C.POINTER(C.c_void_p), C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                                              _I64P]),
     "trust_tc_model_floats": (C.c_int, []),
     "trust_tc_model_init": (C.c_int, [_P, C.c_uint64]),
     "trust_tc_model_grad": (C.c_int, [_P, _P, C.c_int64, _P, _P, C.POINTER(C.c_float)]),

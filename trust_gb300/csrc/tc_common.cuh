@@ -44,7 +44,7 @@ struct TcControl {
   int class_count[TC_NUM_CLASSES];    // list sizes after classification
   int class_cursor[TC_NUM_CLASSES];   // scatter cursors of the classification pass
   int class_next[TC_NUM_CLASSES];     // work-queue heads (atomic chunk claims)
-  int pad[8];
+  int class_off[TC_NUM_CLASSES];      // list offsets, when computed on the device (batches)
 };
 
 #if defined(__CUDACC__)

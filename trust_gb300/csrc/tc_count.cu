@@ -358,6 +358,78 @@ __global__ void class_kernel(const int64_t *__restrict__ begA, const int64_t *__
   (void)lane;
 }
 
+// Batch classification: the key of a row is (size class of its graph, degree class), with the
+// size class's own thresholds; PASS 0 counts into ctl[s].class_count, PASS 1 scatters at
+// ctl[s].class_off (set by batch_offsets_kernel) through ctl[s].class_cursor.
+template <int PASS>
+__global__ void batch_class_kernel(const int64_t *__restrict__ beg, int64_t rows, const int *__restrict__ graph_of,
+                                   const unsigned char *__restrict__ graph_sc, BatchThresholds th, TcControl *ctl,
+                                   int *__restrict__ lists) {
+  constexpr int K = TC_BATCH_CLASSES * TC_NUM_CLASSES;
+  __shared__ int s_hist[K];
+  __shared__ int s_base[K];
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < rows; base += stride) {
+    for (int i = threadIdx.x; i < K; i += blockDim.x) s_hist[i] = 0;
+    __syncthreads();
+    const int64_t v = base + threadIdx.x;
+    int key = -1;
+    if (v < rows) {
+      const int d = (int)(tc_ld_nc(beg + v + 1) - tc_ld_nc(beg + v));
+      const int sc = graph_sc[graph_of[v]];
+      const int c = classify(d, d, 2, th.warp_max[sc], th.cta_max[sc], 0);
+      if (c > TC_CLASS_SKIP) key = sc * TC_NUM_CLASSES + c;
+    }
+    const unsigned peers = __match_any_sync(TC_FULL_MASK, key);
+    const int rank = __popc(peers & tc_lanemask_lt());
+    int wbase = 0;
+    if (key >= 0 && rank == 0) wbase = atomicAdd(&s_hist[key], __popc(peers));
+    wbase = __shfl_sync(TC_FULL_MASK, wbase, __ffs(peers) - 1);
+    __syncthreads();
+    for (int i = threadIdx.x; i < K; i += blockDim.x) {
+      if (!s_hist[i]) continue;
+      TcControl &cs = ctl[i / TC_NUM_CLASSES];
+      if (PASS == 0) atomicAdd(&cs.class_count[i % TC_NUM_CLASSES], s_hist[i]);
+      else s_base[i] = atomicAdd(&cs.class_cursor[i % TC_NUM_CLASSES], s_hist[i]);
+    }
+    __syncthreads();
+    if (PASS == 1 && key >= 0)
+      lists[ctl[key / TC_NUM_CLASSES].class_off[key % TC_NUM_CLASSES] + s_base[key] + wbase + rank] = (int)v;
+    __syncthreads();
+  }
+}
+
+// List offsets of every (size class, degree class), in that order, from the histogram.
+__global__ void batch_offsets_kernel(TcControl *ctl, int nsc) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  int run = 0;
+  for (int s = 0; s < nsc; ++s)
+    for (int c = 0; c < TC_NUM_CLASSES; ++c) {
+      ctl[s].class_off[c] = run;
+      if (c > TC_CLASS_SKIP) run += ctl[s].class_count[c];
+    }
+}
+
+int launch_batch_classify(int pass, const int64_t *beg, int64_t rows, const int *graph_of,
+                          const unsigned char *graph_sc, const BatchThresholds &th, TcControl *ctl, int *lists,
+                          int num_sms, cudaStream_t st) {
+  const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((rows + 255) / 256, (int64_t)num_sms * 8));
+  if (pass == 0)
+    batch_class_kernel<0><<<blocks, 256, 0, st>>>(beg, rows, graph_of, graph_sc, th, ctl, lists);
+  else
+    batch_class_kernel<1><<<blocks, 256, 0, st>>>(beg, rows, graph_of, graph_sc, th, ctl, lists);
+  TC_NOTE_LAUNCH();
+  TC_CUDA_TRY(cudaGetLastError());
+  return TRUST_TC_OK;
+}
+
+int launch_batch_offsets(TcControl *ctl, int nsc, cudaStream_t st) {
+  batch_offsets_kernel<<<1, 32, 0, st>>>(ctl, nsc);
+  TC_NOTE_LAUNCH();
+  TC_CUDA_TRY(cudaGetLastError());
+  return TRUST_TC_OK;
+}
+
 // ------------------------------------------------------------------------------------------
 // the persistent counting kernel
 // ------------------------------------------------------------------------------------------
@@ -410,6 +482,35 @@ __device__ __forceinline__ void row_of(const int64_t *__restrict__ beg, int v, i
   const long long lo = tc_ld_nc(beg + v), hi = tc_ld_nc(beg + v + 1);
   b = (int)lo;
   d = (int)(hi - lo);
+}
+
+// The list of class c (offsets from the host, or computed on the device for batches).
+__device__ __forceinline__ const int *class_list(const CountArgs &p, int c) {
+  return p.lists + (p.dev_off ? p.ctl->class_off[c] : p.off.off[c]);
+}
+
+// Per-graph attribution of a batch.  Every lane keeps the hits of the graph its warp is
+// currently working on; when the warp moves to another graph the warp's sum goes to that graph's
+// counter with one atomic.  Calls are warp-uniform (same g in every lane).
+struct BatchAcc {
+  int cur;
+  unsigned long long h;
+};
+
+__device__ __forceinline__ void batch_flush(const CountArgs &p, BatchAcc &a) {
+  unsigned long long s = a.h;
+#pragma unroll
+  for (int off = 16; off >= 1; off >>= 1) s += __shfl_xor_sync(TC_FULL_MASK, s, off);
+  if ((threadIdx.x & 31) == 0 && a.cur >= 0 && s) atomicAdd(p.graph_counts + a.cur, s);
+  a.h = 0;
+}
+
+__device__ __forceinline__ void batch_take(const CountArgs &p, BatchAcc &a, int g, unsigned long long delta) {
+  if (g != a.cur) {
+    batch_flush(p, a);
+    a.cur = g;
+  }
+  a.h += delta;
 }
 
 // One vertex handled by a whole CTA.  `tab` is shared (CTA class) or global (huge class).
@@ -541,13 +642,13 @@ struct GroupStage {
 // step t+3's row bounds are in flight (the reference walks this chain serially per vertex).
 template <int G, bool SAME, bool REC>
 __device__ void drain_group_class(const CountArgs &p, int c, int *warp_tab, unsigned long long &hits,
-                                  unsigned long long &wedges) {
+                                  unsigned long long &wedges, BatchAcc &acc) {
   constexpr int GPW = 32 / G;
   const int lane = threadIdx.x & 31;
   const int g = lane / G;
   const int glane = lane & (G - 1);
   const int n_items = p.ctl->class_count[c];
-  const int *list = p.lists + p.off.off[c];
+  const int *list = class_list(p, c);
   const int claim = p.chunk * GPW;
   // stage loaders
   auto ld_v = [&](int item, int t1) { return item < t1 ? list[item] : -1; };
@@ -593,7 +694,22 @@ __device__ void drain_group_class(const CountArgs &p, int c, int *warp_tab, unsi
       ld_elem(s2);
       ld_row(s3);
       const long long t_start = REC ? clock64() : 0;
-      group_vertex<G, SAME>(p, s0.uA, s0.s, s0.dd, warp_tab, hits, wedges);
+      if (!p.graph_of) {
+        group_vertex<G, SAME>(p, s0.uA, s0.s, s0.dd, warp_tab, hits, wedges);
+      } else {
+        // a batch: one pass per graph present in this step (almost always one), the other
+        // groups' vertices masked out, so every hit of a pass belongs to that pass's graph
+        const int gid = s0.v >= 0 ? p.graph_of[s0.v] : -1;
+        unsigned pending = __ballot_sync(TC_FULL_MASK, gid >= 0);
+        while (pending) {
+          const int gx = __shfl_sync(TC_FULL_MASK, gid, __ffs(pending) - 1);
+          const bool mine = gid == gx;
+          const unsigned long long h0 = hits;
+          group_vertex<G, SAME>(p, mine ? s0.uA : -1, s0.s, mine ? s0.dd : 0, warp_tab, hits, wedges);
+          batch_take(p, acc, gx, hits - h0);
+          pending &= ~__ballot_sync(TC_FULL_MASK, mine);
+        }
+      }
       if (REC) {
         // the step's cycles, shared among its vertices in proportion to their wedges
         const long long dt = clock64() - t_start;
@@ -625,13 +741,14 @@ __global__ void __launch_bounds__(MAXT, MINB) count_kernel(CountArgs p) {
   const int warp = threadIdx.x >> 5;
   if (threadIdx.x == 0) bs.count = bs.wedges = 0;
   unsigned long long hits = 0, wedges = 0;
+  BatchAcc acc{-1, 0};
 
   // Phase A: CTA-granularity vertices, largest class first.
   for (int c = TC_CLASS_HUGE; c >= TC_CLASS_CTA; --c) {
     const int n_items = p.ctl->class_count[c];
     if (n_items == 0) continue;
     if (c == TC_CLASS_HUGE && (int)blockIdx.x >= p.huge_blocks) continue;
-    const int *list = p.lists + p.off.off[c];
+    const int *list = class_list(p, c);
     int *tab = (c == TC_CLASS_HUGE) ? p.huge_tables + (size_t)blockIdx.x * ((size_t)1 << p.huge_log2)
                                     : smem;
     for (;;) {
@@ -642,8 +759,10 @@ __global__ void __launch_bounds__(MAXT, MINB) count_kernel(CountArgs p) {
       if (t >= n_items) break;
       const int v = list[t];
       const long long t_start = REC ? clock64() : 0;
+      const unsigned long long h0 = hits;
       cta_vertex<SAME>(p, v, tab, bs, hits, wedges);
       if (REC && threadIdx.x == 0) p.cycles[v] = (unsigned long long)(clock64() - t_start);
+      if (p.graph_of) batch_take(p, acc, p.graph_of[v], hits - h0);
     }
   }
   __syncthreads();
@@ -653,7 +772,7 @@ __global__ void __launch_bounds__(MAXT, MINB) count_kernel(CountArgs p) {
   {
     const int c = TC_CLASS_WARP;
     const int n_items = p.ctl->class_count[c];
-    const int *list = p.lists + p.off.off[c];
+    const int *list = class_list(p, c);
     for (;;) {
       int t0 = 0;
       // warp-class vertices are large: claim them one at a time unless the chunk is very coarse
@@ -665,15 +784,18 @@ __global__ void __launch_bounds__(MAXT, MINB) count_kernel(CountArgs p) {
       for (int t = t0; t < t1; ++t) {
         const int v = list[t];
         const long long t_start = REC ? clock64() : 0;
+        const unsigned long long h0 = hits;
         warp_vertex<SAME>(p, v, warp_tab, hits, wedges);
         if (REC && lane == 0) p.cycles[v] = (unsigned long long)(clock64() - t_start);
+        if (p.graph_of) batch_take(p, acc, p.graph_of[v], hits - h0);
       }
     }
   }
-  drain_group_class<32, SAME, REC>(p, TC_CLASS_G32, warp_tab, hits, wedges);
-  drain_group_class<16, SAME, REC>(p, TC_CLASS_G16, warp_tab, hits, wedges);
-  drain_group_class<8, SAME, REC>(p, TC_CLASS_G8, warp_tab, hits, wedges);
-  drain_group_class<4, SAME, REC>(p, TC_CLASS_G4, warp_tab, hits, wedges);
+  drain_group_class<32, SAME, REC>(p, TC_CLASS_G32, warp_tab, hits, wedges, acc);
+  drain_group_class<16, SAME, REC>(p, TC_CLASS_G16, warp_tab, hits, wedges, acc);
+  drain_group_class<8, SAME, REC>(p, TC_CLASS_G8, warp_tab, hits, wedges, acc);
+  drain_group_class<4, SAME, REC>(p, TC_CLASS_G4, warp_tab, hits, wedges, acc);
+  if (p.graph_of) batch_flush(p, acc);
 
   // Reduction: warp shuffle -> shared u64 -> one global u64 atomic per CTA
   // (the reference does per-thread shared atomics, Without-graph-partition/TC.cu:586-599).

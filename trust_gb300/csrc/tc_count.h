@@ -29,6 +29,11 @@ struct CountArgs {
   const int *rowmap;  // optional: table row (A) of each work row (B); null = the same index
   int2 *long_rows;    // optional: per-CTA lists of deferred long neighbour rows (row start, length)
   int long_cap;       // entries per CTA in long_rows (>= the largest CTA-class out-degree)
+  // batches (the disjoint union of many graphs): graph of every row, per-graph counts (both null
+  // otherwise), and list offsets read from ctl->class_off on the device instead of `off`
+  const int *graph_of;
+  unsigned long long *graph_counts;
+  int dev_off;
 };
 
 int launch_check(const int64_t *beg, const int32_t *adj, int64_t rows, int64_t m, int64_t id_bound,
@@ -37,6 +42,16 @@ int launch_classify(int pass, const int64_t *begA, const int64_t *begB, int64_t 
                     int warp_max, int cta_max, TcControl *ctl, int *lists, const ListOffsets &off,
                     int num_sms, cudaStream_t st, int schedule = TRUST_TC_SCHED_TUNED,
                     const int *rowmap = nullptr, const unsigned char *dec = nullptr);
+// batches: graphs fall into TC_BATCH_CLASSES size classes, each with its own degree thresholds
+constexpr int TC_BATCH_CLASSES = 4;
+struct BatchThresholds {
+  int warp_max[TC_BATCH_CLASSES];
+  int cta_max[TC_BATCH_CLASSES];
+};
+int launch_batch_classify(int pass, const int64_t *beg, int64_t rows, const int *graph_of,
+                          const unsigned char *graph_sc, const BatchThresholds &th, TcControl *ctl, int *lists,
+                          int num_sms, cudaStream_t st);
+int launch_batch_offsets(TcControl *ctl, int nsc, cudaStream_t st);
 int count_kernel_occupancy(bool same, int threads, size_t smem_bytes, int *blocks_per_sm);
 // Shared-memory carveout hint: just enough for `per_sm` resident CTAs of `smem_bytes` each.
 int set_count_kernel_carveout(bool same, int threads, size_t smem_bytes, int per_sm);

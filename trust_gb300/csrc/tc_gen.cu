@@ -68,6 +68,37 @@ __global__ void er_kernel(int64_t n, int64_t np, u64 key, int32_t *out) {
   }
 }
 
+// Barabasi-Albert preferential attachment with d edges per vertex, in the endpoint-copy form of
+// Batagelj & Brandes (2005), "Efficient generation of large random networks", made parallel as
+// in Sanders & Schulz (2016), "Scalable generation of scale-free graphs": endpoint position 2e is
+// the source of edge e (vertex e / d), position 2e + 1 its target.  Vertex 0's d edges are self
+// loops (the seed graph).  Edge e of vertex v >= 1 draws a position r uniformly among the 2 v d
+// endpoints of earlier vertices' edges: an even r is the source (r/2)/d, an odd r is the target
+// of edge (r-1)/2, found the same way.  The chain strictly decreases (expected length 2), so
+// every target is a pure function of (seed, e) and any launch shape gives the same pairs.
+__host__ __device__ __forceinline__ u64 mulhi64(u64 a, u64 b) {
+#if defined(__CUDA_ARCH__)
+  return __umul64hi(a, b);
+#else
+  return (u64)(((unsigned __int128)a * b) >> 64);
+#endif
+}
+
+__host__ __device__ __forceinline__ u64 ba_target(u64 key, u64 e, u64 d) {
+  for (;;) {
+    const u64 v = e / d;
+    if (v == 0) return 0;
+    const u64 r = mulhi64(draw(key, e, 0), 2 * v * d);
+    if ((r & 1) == 0) return (r >> 1) / d;
+    e = r >> 1;
+  }
+}
+
+__global__ void ba_kernel(int64_t np, int d, u64 key, int32_t *out) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < np; e += (int64_t)gridDim.x * blockDim.x)
+    reinterpret_cast<int2 *>(out)[e] = make_int2((int)(e / d), (int)ba_target(key, (u64)e, (u64)d));
+}
+
 static int gen_grid(int64_t np) { return (int)std::max<int64_t>(1, std::min<int64_t>((np + 255) / 256, 152 * 64)); }
 
 }  // namespace tc
@@ -129,10 +160,10 @@ int trust_tc_gen_chung_lu_device(trust_tc_ctx *ctx, int64_t n, double gamma, dou
   trust_tc_chung_lu_table(n, gamma, w_max, target_edges, cdf.data());
   uint64_t *d_cdf = nullptr;
   TC_CUDA_TRY(cudaMalloc(&d_cdf, sizeof(uint64_t) * (size_t)n));
-  TC_NOTE_LAUNCH();
   cudaError_t e = cudaMemcpy(d_cdf, cdf.data(), sizeof(uint64_t) * (size_t)n, cudaMemcpyHostToDevice);
   if (e == cudaSuccess && npairs) {
     weighted_kernel<<<gen_grid(npairs), 256>>>((const u64 *)d_cdf, n, npairs, gen_key(seed), d_pairs);
+    TC_NOTE_LAUNCH();
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) e = cudaDeviceSynchronize();
@@ -143,9 +174,23 @@ int trust_tc_gen_chung_lu_device(trust_tc_ctx *ctx, int64_t n, double gamma, dou
 
 int trust_tc_gen_er_device(trust_tc_ctx *ctx, int64_t n, int64_t npairs, uint64_t seed, int32_t *d_pairs) {
   if (n < 1 || n >= ((int64_t)1 << 31) || npairs < 0 || (npairs && !d_pairs)) return TRUST_TC_E_ARG;
-TC_NOTE_LAUNCH();
   if (ctx) TC_CUDA_TRY(cudaSetDevice(ctx->device));
-  if (npairs) er_kernel<<<gen_grid(npairs), 256>>>(n, npairs, gen_key(seed), d_pairs);
+  if (npairs) {
+    er_kernel<<<gen_grid(npairs), 256>>>(n, npairs, gen_key(seed), d_pairs);
+    TC_NOTE_LAUNCH();
+  }
+  TC_CUDA_TRY(cudaGetLastError());
+  TC_CUDA_TRY(cudaDeviceSynchronize());
+  return TRUST_TC_OK;
+}
+
+int trust_tc_gen_ba_device(trust_tc_ctx *ctx, int64_t n, int d, uint64_t seed, int32_t *d_pairs) {
+  if (n < 1 || n >= ((int64_t)1 << 31) || d < 1 || n * (int64_t)d >= ((int64_t)1 << 40) || !d_pairs)
+    return TRUST_TC_E_ARG;
+  if (ctx) TC_CUDA_TRY(cudaSetDevice(ctx->device));
+  const int64_t np = n * (int64_t)d;
+  ba_kernel<<<gen_grid(np), 256>>>(np, d, gen_key(seed), d_pairs);
+  TC_NOTE_LAUNCH();
   TC_CUDA_TRY(cudaGetLastError());
   TC_CUDA_TRY(cudaDeviceSynchronize());
   return TRUST_TC_OK;

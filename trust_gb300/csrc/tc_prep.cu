@@ -338,8 +338,22 @@ struct DevBufs {
   }
 };
 
+// seg_out[g] = compacted id of the first vertex at or after original id seg_in[g] (the present
+// vertices before it), or n for seg_in[g] >= id_bound
+__global__ void seg_map_kernel(const u32 *__restrict__ cid, int64_t id_bound, int64_t n,
+                               const int64_t *__restrict__ seg_in, int64_t nseg, int64_t *seg_out) {
+  GRID_STRIDE(g, nseg) {
+    const int64_t x = seg_in[g];
+    seg_out[g] = x >= id_bound ? n : (x <= 0 ? 0 : (int64_t)cid[x]);
+  }
+}
+
+// keep_order: new ids are the compacted ids (original order kept, isolated vertices dropped)
+// instead of the out-degree-descending renumbering; with d_seg_in / d_seg_out (nseg entries, on
+// the device) the original-id boundaries of segments are mapped to the new ids.
 int build_csr_device(const int32_t *d_pairs, int64_t np, int64_t id_bound, int64_t **d_beg_out,
-                     int32_t **d_adj_out, int64_t *n_out, int64_t *m_out, cudaStream_t st) {
+                     int32_t **d_adj_out, int64_t *n_out, int64_t *m_out, cudaStream_t st, bool keep_order,
+                     const int64_t *d_seg_in, int64_t nseg, int64_t *d_seg_out) {
   if (np < 0 || id_bound < 1 || id_bound >= ((int64_t)1 << 31)) return TRUST_TC_E_ARG;
   if (np >= ((int64_t)1 << 32) - 1) return TRUST_TC_E_TOO_LARGE;
   DevBufs B;
@@ -399,7 +413,12 @@ int build_csr_device(const int32_t *d_pairs, int64_t np, int64_t id_bound, int64
   TC_CUDA_TRY(cudaMemsetAsync(od, 0, sizeof(u32) * n, st));
   orient_kernel<<<grid_for(nu), 256, 0, st>>>(e, nu, cid, vpos, od);
   TC_NOTE_LAUNCH();
+  if (d_seg_in && nseg > 0) {
+    seg_map_kernel<<<grid_for(nseg), 256, 0, st>>>(cid, id_bound, n, d_seg_in, nseg, d_seg_out);
+    TC_NOTE_LAUNCH();
+  }
   // 6. renumber: out-degree descending, ties by compacted id
+  if (!keep_order) {
   TC_CUDA_TRY(cudaMemsetAsync(dmax, 0, sizeof(u32), st));
   max_kernel<<<grid_for(n), 256, 0, st>>>(od, n, dmax);
   TC_NOTE_LAUNCH();
@@ -413,9 +432,10 @@ int build_csr_device(const int32_t *d_pairs, int64_t np, int64_t id_bound, int64
   push_digits(sh, 32, bits_for(hodmax));
   if ((rc = radix_sort(vkeys, vtmp, n, sh, st))) return rc;
   position_kernel<<<grid_for(n), 256, 0, st>>>(vkeys, n, vpos);  // vpos = new id of compacted id
+  TC_NOTE_LAUNCH();
   relabel_kernel<<<grid_for(nu), 256, 0, st>>>(e, nu, vpos);
   TC_NOTE_LAUNCH();
-  TC_NOTE_LAUNCH();
+  }
   // 7. sort arcs by (source, target) and emit the CSR
   sh.clear();
   push_digits(sh, 0, bits_for(std::max<int64_t>(n - 1, 1)));
@@ -463,7 +483,35 @@ extern "C" int trust_tc_build_csr_device(trust_tc_ctx *ctx, const int32_t *d_pai
   *d_begin = nullptr;
   *d_adj = nullptr;
   if (ctx) TC_CUDA_TRY(cudaSetDevice(ctx->device));
-  return tc::build_csr_device(d_pairs, npairs, id_bound, d_begin, d_adj, n, m, (cudaStream_t)0);
+  return tc::build_csr_device(d_pairs, npairs, id_bound, d_begin, d_adj, n, m, (cudaStream_t)0, false, nullptr, 0,
+                              nullptr);
+}
+
+extern "C" int trust_tc_build_batch_device(trust_tc_ctx *ctx, const int32_t *d_pairs, int64_t npairs,
+                                           const int64_t *graph_vbeg, int64_t num_graphs, int64_t **d_begin,
+                                           int32_t **d_adj, int64_t *n, int64_t *m, int64_t *graph_vbeg_out) {
+  if (!d_begin || !d_adj || !n || !m || (npairs > 0 && !d_pairs) || num_graphs < 1 || !graph_vbeg ||
+      !graph_vbeg_out || graph_vbeg[0] != 0)
+    return TRUST_TC_E_ARG;
+  for (int64_t g = 0; g < num_graphs; ++g)
+    if (graph_vbeg[g] > graph_vbeg[g + 1]) return TRUST_TC_E_ARG;
+  *d_begin = nullptr;
+  *d_adj = nullptr;
+  if (ctx) TC_CUDA_TRY(cudaSetDevice(ctx->device));
+  const int64_t nseg = num_graphs + 1;
+  int64_t *d_seg = nullptr;
+  TC_CUDA_TRY(cudaMalloc((void **)&d_seg, sizeof(int64_t) * 2 * (size_t)nseg));
+  cudaError_t e = cudaMemcpy(d_seg, graph_vbeg, sizeof(int64_t) * (size_t)nseg, cudaMemcpyHostToDevice);
+  int rc = e == cudaSuccess ? TRUST_TC_OK : tc::cuda_status(e);
+  if (!rc)
+    rc = tc::build_csr_device(d_pairs, npairs, std::max<int64_t>(graph_vbeg[num_graphs], 1), d_begin, d_adj, n, m,
+                              (cudaStream_t)0, true, d_seg, nseg, d_seg + nseg);
+  if (!rc) {
+    e = cudaMemcpy(graph_vbeg_out, d_seg + nseg, sizeof(int64_t) * (size_t)nseg, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) rc = tc::cuda_status(e);
+  }
+  cudaFree(d_seg);
+  return rc;
 }
 
 extern "C" void trust_tc_free_device(void *p) {
