@@ -214,6 +214,43 @@ double trust_tc_chung_lu_table(int64_t n, double gamma, double w_max, int64_t ta
 int trust_tc_gen_er_device(trust_tc_ctx *ctx, int64_t n, int64_t npairs, uint64_t seed,
                            int32_t *d_pairs);
 
+/* ---- batches: many graphs counted by one CUDA-graph launch -------------------------------
+ * A batch is the disjoint union of many oriented graphs in one device CSR (ids global), graph g
+ * owning rows [graph_vbeg[g], graph_vbeg[g+1]) and no arc leaving its graph (build it with
+ * trust_tc_build_batch_device).  Graphs fall into TRUST_TC_BATCH_CLASSES size classes by vertex
+ * count ([0,512), [512,4096), [4096,32768), [32768,...)), each counted by its own persistent
+ * kernel with its own launch parameters; validation, classification, list offsets, the kernels
+ * and the readback of the per-graph counts are captured in one CUDA graph at creation and
+ * replayed by every run.  No counterpart in the reference, which counts one graph per run
+ * (Without-graph-partition/mpi_main.cpp:90-124); the per-graph counts equal its counts. */
+#define TRUST_TC_BATCH_CLASSES 4
+typedef struct trust_tc_batch_class {
+  int threads_per_block; /* 64..1024, multiple of 32 (default 256)                            */
+  int warp_max_degree;   /* out-degree above which a vertex gets a whole CTA (default 128)     */
+  int chunk;             /* vertices per queue claim (default 8)                               */
+} trust_tc_batch_class;
+typedef struct trust_tc_batch trust_tc_batch;
+
+/* Validates the union (offsets, ids, no arc across graphs), then plans and captures the job.
+ * The batch borrows d_begin / d_adj and the context; graph_vbeg is a host array. */
+int trust_tc_batch_create(trust_tc_ctx *ctx, const int64_t *d_begin, const int32_t *d_adj, int64_t n,
+                          int64_t m, const int64_t *graph_vbeg, int64_t num_graphs, trust_tc_batch **out);
+void trust_tc_batch_destroy(trust_tc_batch *batch);
+/* graphs, vertices and largest out-degree of every size class (TRUST_TC_BATCH_CLASSES each) */
+int trust_tc_batch_info(const trust_tc_batch *batch, int64_t *graphs, int64_t *vertices,
+                        int32_t *max_out_degree);
+int trust_tc_batch_get_class(const trust_tc_batch *batch, int size_class, trust_tc_batch_class *cfg);
+/* sets one size class's launch parameters and re-captures the job */
+int trust_tc_batch_set_class(trust_tc_batch *batch, int size_class, const trust_tc_batch_class *cfg);
+/* Times every size class's kernel under each candidate (threads 128/256/512/1024 x warp bound
+ * 64/128 x chunk 2/4/8/16, `repeats` runs each, fastest kept), keeps the fastest configuration
+ * per class and re-captures the job; *best_ms = the sum of the chosen kernels' times. */
+int trust_tc_batch_autotune(trust_tc_batch *batch, int repeats, double *best_ms);
+/* One launch of the captured job on `stream` (waits for it).  counts: host array of num_graphs
+ * uint64 per-graph triangle counts (or NULL); result: totals, call_seconds = the graph's
+ * CUDA-event time. */
+int trust_tc_batch_run(trust_tc_batch *batch, void *stream, uint64_t *counts, trust_tc_result *result);
+
 /* ---- the learned schedule's per-vertex cost model ----------------------------------------
  * An MLP, 8 fp32 features -> 32 -> 32 -> 1 (ReLU), predicting log2 of a vertex's counting cycles.
  * Features of a vertex v with out-degree d(v) >= 2 (trust_tc_vertex_features):

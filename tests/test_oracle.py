@@ -143,3 +143,30 @@ def test_generators_deterministic():
     assert np.all(np.diff(cdf.astype(np.float64)) >= 0) and int(cdf[-1]) == 1 << 63
     w = O.gen_weighted(cdf, 4000, seed=9)
     assert w.min() >= 0 and w.max() < 5000
+
+
+def test_ba_oracle_structure():
+    """Barabasi-Albert pairs: vertex v's d pairs come from v, and every target is an earlier
+    vertex (vertex 0's pairs are the self-loop seed)."""
+    n, d = 3000, 5
+    p = O.gen_ba(n, d, 9)
+    assert p.shape == (n * d, 2)
+    assert np.array_equal(p[:, 0], np.repeat(np.arange(n), d))
+    assert np.all(p[:d] == 0)
+    assert np.all(p[d:, 1] < p[d:, 0])
+    deg = np.bincount(p[d:].ravel(), minlength=n)
+    assert deg.max() > 10 * d  # preferential attachment grows hubs
+    assert np.array_equal(p, O.gen_ba(n, d, 9)) and not np.array_equal(p, O.gen_ba(n, d, 10))
+
+
+def test_batch_specs_stream():
+    """The batch workload's graph list comes from a counter-based stream: pinned values."""
+    from trust_gb300.batch import batch_specs
+    s = batch_specs()
+    assert len(s) == 4096
+    assert [(x.kind, x.n, x.param) for x in s[:4]] == [("er", 102, 27), ("ba", 60, 9), ("er", 14261, 27),
+                                                        ("ba", 65, 2)]
+    ns = np.array([x.n for x in s])
+    assert ns.min() >= 50 and ns.max() <= 50_000
+    assert sum(x.kind == "er" for x in s) == 2048
+    assert all(4 <= x.param <= 64 for x in s if x.kind == "er") and all(2 <= x.param <= 16 for x in s if x.kind == "ba")

@@ -27,7 +27,7 @@ from ._lib import (CLASS_NAMES, DEVICE, HOST, SCHED_LEARNED, SCHED_PLAIN, SCHED_
 __all__ = [
     "arguments", "Triangle_count", "Context", "CountResult", "count_csr", "count_folder", "count_partitioned",
     "load_folder", "save_folder", "partition_folder", "gen_rmat", "gen_chung_lu", "gen_er", "build_csr",
-    "chung_lu_table", "TrustTcError", "load", "model_floats", "model_init", "model_default", "model_grad",
+    "chung_lu_table", "gen_ba", "TrustTcError", "load", "model_floats", "model_init", "model_default", "model_grad",
     "model_train", "model_predict", "vertex_features",
 ]
 
@@ -234,6 +234,13 @@ def gen_chung_lu(n: int, gamma: float, w_max: float, target_edges: int, npairs: 
     out = _pairs(npairs)
     check(load().trust_tc_gen_chung_lu_device(None, n, gamma, w_max, target_edges, npairs, seed,
                                               C.c_void_p(out.data_ptr())), "trust_tc_gen_chung_lu_device")
+    return out
+
+
+def gen_ba(n: int, d: int, seed=5):
+    """Barabasi-Albert pairs on the GPU: (n * d) x 2 int32 tensor (vertex 0's d pairs are self loops)."""
+    out = _pairs(n * d)
+    check(load().trust_tc_gen_ba_device(None, n, d, seed, C.c_void_p(out.data_ptr())), "trust_tc_gen_ba_device")
     return out
 
 

@@ -53,6 +53,12 @@ class Result(C.Structure):
     ]
 
 
+class BatchClass(C.Structure):
+    _fields_ = [("threads_per_block", C.c_int), ("warp_max_degree", C.c_int), ("chunk", C.c_int)]
+
+
+BATCH_CLASSES = 4
+
 _P = C.c_void_p
 _I64P = C.POINTER(C.c_int64)
 _I32P = C.POINTER(C.c_int32)
@@ -87,6 +93,13 @@ SIGNATURES = {
     "trust_tc_chung_lu_table": (C.c_double, [C.c_int64, C.c_double, C.c_double, C.c_int64, _P]),
     "trust_tc_gen_er_device": (C.c_int, [_P, C.c_int64, C.c_int64, C.c_uint64, _P]),
     "trust_tc_gen_ba_device": (C.c_int, [_P, C.c_int64, C.c_int, C.c_uint64, _P]),
+    "trust_tc_batch_create": (C.c_int, [_P, _P, _P, C.c_int64, C.c_int64, _I64P, C.c_int64, C.POINTER(C.c_void_p)]),
+    "trust_tc_batch_destroy": (None, [_P]),
+    "trust_tc_batch_info": (C.c_int, [_P, _I64P, _I64P, _I32P]),
+    "trust_tc_batch_get_class": (C.c_int, [_P, C.c_int, C.POINTER(BatchClass)]),
+    "trust_tc_batch_set_class": (C.c_int, [_P, C.c_int, C.POINTER(BatchClass)]),
+    "trust_tc_batch_autotune": (C.c_int, [_P, C.c_int, C.POINTER(C.c_double)]),
+    "trust_tc_batch_run": (C.c_int, [_P, _P, C.POINTER(C.c_uint64), C.POINTER(Result)]),
     "trust_tc_build_batch_device": (C.c_int, [_P, _P, C.c_int64, _I64P, C.c_int64, C.POINTER(C.c_void_p),
                                               C.POINTER(C.c_void_p), C.POINTER(C.c_int64), C.POINTER(C.c_int64),
                                               _I64P]),

@@ -33,7 +33,7 @@ ORACLE_CUDA_LIB = os.path.join(ORACLE_OBJ, "liboracle_cuda.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off", "-I" + INCLUDE]
-SOURCES = ["tc_count.cu", "tc_prep.cu", "tc_gen.cu", "tc_api.cpp", "tc_tiles.cpp", "tc_shim.cpp", "tc_noalloc.cu", "tc_split.cu", "tc_model.cu"]
+SOURCES = ["tc_count.cu", "tc_prep.cu", "tc_gen.cu", "tc_api.cpp", "tc_tiles.cpp", "tc_shim.cpp", "tc_noalloc.cu", "tc_split.cu", "tc_model.cu", "tc_batch.cu"]
 
 
 def _cuda_home() -> str:

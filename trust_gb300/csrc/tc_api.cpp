@@ -26,7 +26,7 @@ namespace tc {
 static thread_local char g_cuda_err[256] = "";
 static std::atomic<uint64_t> g_kernel_launches{0};
 
-void note_launch() { g_kernel_launches.fetch_add(1, std::memory_order_relaxed); }
+void note_launch(uint64_t k) { g_kernel_launches.fetch_add(k, std::memory_order_relaxed); }
 
 int cuda_status(cudaError_t e) {
   if (e == cudaSuccess) return TRUST_TC_OK;

@@ -69,7 +69,7 @@ __device__ __forceinline__ long long tc_ld_nc(const int64_t *p) {
 // Host helpers shared by the translation units.
 namespace tc {
 int cuda_status(cudaError_t e);  // records the text, returns TRUST_TC_E_CUDA (or OK)
-void note_launch();              // one more kernel launched by the library
+void note_launch(uint64_t k = 1);  // k more kernels launched by the library
 }
 
 // After every kernel launch of the library (trust_tc_kernel_launches reports the total).
