@@ -162,6 +162,13 @@ int trust_tc_count_folder(const char *folder, const trust_tc_opts *opts, trust_t
  * unpartitioned count. */
 int trust_tc_count_partitioned(const char *folder, int parts, const trust_tc_opts *opts,
                                trust_tc_result *result);
+/* The same tile loop for a device-resident CSR: the GPU splits it into parts x parts tiles (the
+ * layout of Preprocess/partition.cpp:72-121, in pinned host memory), then the (i,j,k) jobs run
+ * with the tiles streamed into a device cache of at most device_budget_bytes (0 = 80 % of free
+ * memory): the larger-than-HBM mode, exercised on any graph by a small budget.  parts <= 32.
+ * result->call_seconds spans the job loop including the tile copies (the partition excluded). */
+int trust_tc_count_tiles_device(const int64_t *d_begin, const int32_t *d_adj, int64_t n, int64_t m, int parts,
+                                size_t device_budget_bytes, const trust_tc_opts *opts, trust_tc_result *r);
 
 /* Split a CSR into parts x parts tiles (row class v%parts, column class w%parts, local id w/parts)
  * and write them as partition<i>_<j>/begin.bin,adjacent.bin under `folder`.  Follows

@@ -44,3 +44,35 @@ def test_tile_loop_rmat16(tmp_path):
     expect = O.count_forward(beg, adj, threads=8)
     T.partition_folder(str(tmp_path), beg, adj, 2)
     assert T.count_partitioned(str(tmp_path), 2).triangles == expect
+
+
+@pytest.mark.parametrize("name", ["toy", "rmat_s12", "k150", "chung_lu_3000", "er_200"])
+@pytest.mark.parametrize("p", [1, 2, 3, 5])
+def test_device_tile_loop_equals_whole_graph(name, p):
+    """The GPU partition of a device CSR and the streamed tile loop give the whole count."""
+    import torch
+    z = np.load(os.path.join(GOLD, name + ".npz"))
+    beg = torch.from_numpy(z["ref_beg"].astype(np.int64)).cuda()
+    adj = torch.from_numpy(z["ref_adj"].astype(np.int32)).cuda()
+    r = T.count_tiles(beg, adj, p)
+    assert r.triangles == int(z["nx_triangles"][0])
+    assert r.edges == adj.numel() and r.vertices == beg.numel() - 1
+
+
+@pytest.mark.parametrize("p,budget", [(2, 1), (2, 0), (4, 1 << 20)])
+def test_device_tile_loop_streams_under_a_budget(p, budget):
+    """A budget smaller than one job's three tiles evicts on every job: same count as in HBM."""
+    pairs = T.gen_rmat(17, 16, seed=4)
+    beg, adj = T.build_csr(pairs, 1 << 17)
+    whole = T.count_csr(beg, adj)
+    r = T.count_tiles(beg, adj, p, budget_bytes=budget)
+    assert r.triangles == whole.triangles
+
+
+def test_device_tile_loop_rejects_bad_ids():
+    import torch
+    beg = torch.tensor([0, 2, 3, 3], dtype=torch.int64, device="cuda")
+    adj = torch.tensor([1, 7, 2], dtype=torch.int32, device="cuda")
+    with pytest.raises(T.TrustTcError) as e:
+        T.count_tiles(beg, adj, 2)
+    assert e.value.status == T._lib.E_IDS

@@ -26,6 +26,7 @@ from ._lib import (CLASS_NAMES, DEVICE, HOST, SCHED_LEARNED, SCHED_PLAIN, SCHED_
 
 __all__ = [
     "arguments", "Triangle_count", "Context", "CountResult", "count_csr", "count_folder", "count_partitioned",
+    "count_tiles",
     "load_folder", "save_folder", "partition_folder", "gen_rmat", "gen_chung_lu", "gen_er", "build_csr",
     "chung_lu_table", "gen_ba", "TrustTcError", "load", "model_floats", "model_init", "model_default", "model_grad",
     "model_train", "model_predict", "vertex_features",
@@ -157,6 +158,18 @@ def count_partitioned(folder: str, parts: int, threads=0, blocks=0, chunk=0) -> 
     r = _lib.Result()
     check(load().trust_tc_count_partitioned(folder.encode(), parts, C.byref(o), C.byref(r)),
           "trust_tc_count_partitioned")
+    return _result(r)
+
+
+def count_tiles(beg, adj, parts: int, budget_bytes: int = 0, threads=0, blocks=0, chunk=0,
+                schedule=SCHED_LEARNED) -> CountResult:
+    """The n x n tile loop over a device CSR (torch CUDA tensors): GPU partition into pinned host
+    tiles, then the (i,j,k) jobs with tiles streamed into a device cache of `budget_bytes`."""
+    o = _opts(threads, blocks, chunk, DEVICE, schedule=schedule)
+    r = _lib.Result()
+    check(load().trust_tc_count_tiles_device(C.c_void_p(beg.data_ptr()), C.c_void_p(adj.data_ptr()), beg.numel() - 1,
+                                             adj.numel(), parts, budget_bytes, C.byref(o), C.byref(r)),
+          "trust_tc_count_tiles_device")
     return _result(r)
 
 

@@ -81,6 +81,8 @@ SIGNATURES = {
     "trust_tc_free_host": (None, [_P]),
     "trust_tc_count_folder": (C.c_int, [C.c_char_p, C.POINTER(Opts), C.POINTER(Result)]),
     "trust_tc_count_partitioned": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(Opts), C.POINTER(Result)]),
+    "trust_tc_count_tiles_device": (C.c_int, [_P, _P, C.c_int64, C.c_int64, C.c_int, C.c_size_t, C.POINTER(Opts),
+                                              C.POINTER(Result)]),
     "trust_tc_partition_folder": (C.c_int, [C.c_char_p, _P, _P, C.c_int64, C.c_int64, C.c_int]),
     "trust_tc_build_csr_device": (C.c_int, [_P, _P, C.c_int64, C.c_int64, C.POINTER(C.c_void_p),
                                             C.POINTER(C.c_void_p), _I64P, _I64P]),

@@ -82,6 +82,14 @@ int ensure(void **p, size_t *cap, size_t bytes);
 int count_device(trust_tc_ctx *c, const DevGraph3 &g, const trust_tc_opts &o, bool check_ids,
                  trust_tc_result *r);
 int scan_exclusive_i64(const int64_t *in, int64_t *out, int64_t n, cudaStream_t st, int64_t *total);
+// The n x n hash partition of a device CSR into p*p tiles (tile i*p+j) in pinned host memory
+// (free each beg / adj with cudaFreeHost); p <= 32.
+struct PinnedTile {
+  int64_t *beg;
+  int32_t *adj;
+  int64_t rows, m;
+};
+int partition_device_to_host(const int64_t *beg, const int32_t *adj, int64_t n, int64_t m, int p, PinnedTile *tiles);
 constexpr int TC_PLAN_WORDS = 8;  // words of the scheduling pass's totals
 struct SchedPlan {
   unsigned long long w_all, w_min;  // probes without / with the direction split

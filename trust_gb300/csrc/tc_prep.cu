@@ -476,6 +476,118 @@ int build_csr_device(const int32_t *d_pairs, int64_t np, int64_t id_bound, int64
 
 }  // namespace tc
 
+// ---- the n x n hash partition on the GPU ---------------------------------------------------
+// Tile (i,j) of Preprocess/partition.cpp:72-121: the rows of vertices v = i (mod p) as local row
+// v / p, restricted to entries w = j (mod p), stored as w / p; rows stay sorted.  A warp per
+// row: one ballot per part and 32 entries, lane j keeps part j's count (pass 1) or cursor (pass 2).
+__global__ void part_count_kernel(const int64_t *__restrict__ beg, const int32_t *__restrict__ adj, int64_t n,
+                                  int p, int64_t stride, int64_t *__restrict__ cnt) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t v = warp; v < n; v += nwarps) {
+    const int64_t b = beg[v], e = beg[v + 1];
+    int64_t mine = 0;
+    for (int64_t k0 = b; k0 < e; k0 += 32) {
+      const bool valid = k0 + lane < e;
+      const int jw = valid ? (int)(adj[k0 + lane] % p) : -1;
+      for (int j = 0; j < p; ++j) {
+        const unsigned msk = __ballot_sync(TC_FULL_MASK, jw == j);
+        if (lane == j) mine += __popc(msk);
+      }
+    }
+    if (lane < p) cnt[(int64_t)((v % p) * p + lane) * stride + v / p] = mine;
+  }
+}
+
+__global__ void part_fill_kernel(const int64_t *__restrict__ beg, const int32_t *__restrict__ adj, int64_t n, int p,
+                                 int64_t stride, const int64_t *__restrict__ off, const int64_t *__restrict__ tbase,
+                                 int32_t *__restrict__ out) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t v = warp; v < n; v += nwarps) {
+    const int64_t b = beg[v], e = beg[v + 1];
+    if (b == e) continue;
+    const int i = (int)(v % p);
+    // lane j: where part j's entries of this row go (tile base + row offset)
+    int64_t pos = lane < p ? tbase[i * p + lane] + off[(int64_t)(i * p + lane) * stride + v / p] : 0;
+    for (int64_t k0 = b; k0 < e; k0 += 32) {
+      const bool valid = k0 + lane < e;
+      const int w = valid ? adj[k0 + lane] : 0;
+      const int jw = valid ? w % p : -1;
+      for (int j = 0; j < p; ++j) {
+        const unsigned msk = __ballot_sync(TC_FULL_MASK, jw == j);
+        const int64_t cur = __shfl_sync(TC_FULL_MASK, pos, j);
+        if (jw == j) out[cur + __popc(msk & ((1u << lane) - 1u))] = w / p;
+        if (lane == j) pos += __popc(msk);
+      }
+    }
+  }
+}
+
+namespace tc {
+
+int partition_device_to_host(const int64_t *beg, const int32_t *adj, int64_t n, int64_t m, int p, PinnedTile *tiles) {
+  if (n < 1 || m < 0 || p < 1 || p > 32) return TRUST_TC_E_ARG;
+  cudaStream_t st = 0;
+  const int64_t stride = (n + p - 1) / p + 1;  // rows of part 0, plus the end offset
+  const size_t T = (size_t)p * p;
+  int64_t *cnt = nullptr, *tbase = nullptr;
+  int32_t *out = nullptr;
+  for (size_t t = 0; t < T; ++t) tiles[t] = PinnedTile{};
+  TC_CUDA_TRY(cudaMalloc((void **)&cnt, sizeof(int64_t) * T * (size_t)stride));
+  auto done = [&](int rc) {
+    cudaFree(cnt);
+    cudaFree(tbase);
+    cudaFree(out);
+    return rc;
+  };
+  auto cu = [&](cudaError_t e) { return e == cudaSuccess ? TRUST_TC_OK : cuda_status(e); };
+  int rc = cu(cudaMemsetAsync(cnt, 0, sizeof(int64_t) * T * (size_t)stride, st));
+  if (rc) return done(rc);
+  const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((n * 32 + 255) / 256, 152 * 64));
+  part_count_kernel<<<blocks, 256, 0, st>>>(beg, adj, n, p, stride, cnt);
+  TC_NOTE_LAUNCH();
+  if ((rc = cu(cudaGetLastError()))) return done(rc);
+  std::vector<int64_t> hbase(T + 1, 0);
+  for (size_t t = 0; t < T; ++t) {
+    const int i = (int)(t / p);
+    const int64_t rows = n > i ? (n - i + p - 1) / p : 0;
+    int64_t total = 0;
+    if ((rc = scan_exclusive_i64(cnt + t * stride, cnt + t * stride, rows + 1, st, &total))) return done(rc);
+    tiles[t].rows = rows;
+    tiles[t].m = total;
+    hbase[t + 1] = hbase[t] + total;
+  }
+  if (hbase[T] != m) return done(TRUST_TC_E_DEVICE);
+  if ((rc = cu(cudaMalloc((void **)&tbase, sizeof(int64_t) * (T + 1))))) return done(rc);
+  if ((rc = cu(cudaMalloc((void **)&out, sizeof(int32_t) * (size_t)std::max<int64_t>(m, 1))))) return done(rc);
+  if ((rc = cu(cudaMemcpy(tbase, hbase.data(), sizeof(int64_t) * (T + 1), cudaMemcpyHostToDevice)))) return done(rc);
+  part_fill_kernel<<<blocks, 256, 0, st>>>(beg, adj, n, p, stride, cnt, tbase, out);
+  TC_NOTE_LAUNCH();
+  if ((rc = cu(cudaGetLastError()))) return done(rc);
+  for (size_t t = 0; t < T; ++t) {
+    PinnedTile &x = tiles[t];
+    if ((rc = cu(cudaMallocHost((void **)&x.beg, sizeof(int64_t) * (size_t)(x.rows + 1))))) break;
+    if ((rc = cu(cudaMallocHost((void **)&x.adj, sizeof(int32_t) * (size_t)std::max<int64_t>(x.m, 1))))) break;
+    if ((rc = cu(cudaMemcpy(x.beg, cnt + t * stride, sizeof(int64_t) * (size_t)(x.rows + 1), cudaMemcpyDeviceToHost))))
+      break;
+    if (x.m && (rc = cu(cudaMemcpy(x.adj, out + hbase[t], sizeof(int32_t) * (size_t)x.m, cudaMemcpyDeviceToHost))))
+      break;
+  }
+  if (rc) {
+    for (size_t t = 0; t < T; ++t) {
+      cudaFreeHost(tiles[t].beg);
+      cudaFreeHost(tiles[t].adj);
+      tiles[t] = PinnedTile{};
+    }
+  }
+  return done(rc);
+}
+
+}  // namespace tc
+
 extern "C" int trust_tc_build_csr_device(trust_tc_ctx *ctx, const int32_t *d_pairs, int64_t npairs,
                                          int64_t id_bound, int64_t **d_begin, int32_t **d_adj, int64_t *n,
                                          int64_t *m) {

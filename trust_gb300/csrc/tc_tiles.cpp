@@ -19,6 +19,7 @@
 #include <string>
 #include <vector>
 
+#include "tc_count.h"
 #include "tc_internal.h"
 
 namespace {
@@ -79,44 +80,27 @@ int trust_tc_partition_folder(const char *folder, const int64_t *beg, const int3
   return TRUST_TC_OK;
 }
 
-int trust_tc_count_partitioned(const char *folder, int parts, const trust_tc_opts *opts, trust_tc_result *r) {
-  if (!folder || !r || parts < 1 || parts > 64) return TRUST_TC_E_ARG;
-  trust_tc_opts o;
-  if (opts) o = *opts; else trust_tc_opts_init(&o);
-  const int p = parts;
-  std::vector<HostTile> ht((size_t)p * p);
+}  // extern "C"
+
+namespace tc {
+
+// The (i,j,k) jobs over p x p host tiles (all p*p present, ht[i*p+j]), the tiles kept in a device
+// cache with an LRU byte budget (0 = 80 % of the free memory at entry).  r->call_seconds covers
+// the whole loop including the host-to-device tile copies.
+int tile_loop(const std::vector<HostTile> &ht, int p, const trust_tc_opts &o, size_t budget_bytes,
+              trust_tc_result *r) {
   int rc = TRUST_TC_OK;
-  auto free_host = [&]() {
-    for (auto &t : ht) {
-      free(t.beg);
-      free(t.adj);
-    }
-  };
   int64_t total_m = 0;
-  for (int i = 0; i < p && !rc; ++i)
-    for (int j = 0; j < p && !rc; ++j) {
-      HostTile &t = ht[(size_t)i * p + j];
-      rc = trust_tc_load_folder(tile_dir(folder, i, j).c_str(), &t.beg, &t.adj, &t.rows, &t.m);
-      total_m += t.m;
-    }
-  for (int i = 0; i < p && !rc; ++i)
-    for (int j = 1; j < p && !rc; ++j)
-      if (ht[(size_t)i * p + j].rows != ht[(size_t)i * p].rows) rc = TRUST_TC_E_FORMAT;
-  if (rc) {
-    free_host();
-    return rc;
-  }
+  for (const auto &t : ht) total_m += t.m;
   trust_tc_ctx ctx;
-  rc = tc::ctx_init(&ctx, o.device);
+  rc = ctx_init(&ctx, o.device);
   if (rc) {
-    tc::ctx_release(&ctx);
-    free_host();
+    ctx_release(&ctx);
     return rc;
   }
-  // device tile cache with an LRU byte budget (80% of free memory at entry)
   size_t free_b = 0, total_b = 0;
   cudaMemGetInfo(&free_b, &total_b);
-  const size_t budget = free_b / 10 * 8;
+  const size_t budget = budget_bytes ? budget_bytes : free_b / 10 * 8;
   std::vector<DevTile> dt((size_t)p * p);
   std::list<int> lru;
   size_t used = 0;
@@ -133,6 +117,7 @@ int trust_tc_count_partitioned(const char *folder, int parts, const trust_tc_opt
     }
     return false;
   };
+  uint64_t copied = 0;
   auto fetch = [&](int id, int k0, int k1, int k2) -> int {
     DevTile &d = dt[id];
     if (d.resident) {
@@ -152,8 +137,9 @@ int trust_tc_count_partitioned(const char *folder, int parts, const trust_tc_opt
       cudaFree(d.beg);
       cudaFree(d.adj);
       d = DevTile();
-      return tc::cuda_status(e);
+      return cuda_status(e);
     }
+    copied += bytes;
     d.bytes = bytes;
     d.resident = true;
     used += bytes;
@@ -164,16 +150,21 @@ int trust_tc_count_partitioned(const char *folder, int parts, const trust_tc_opt
   memset(r, 0, sizeof *r);
   r->vertex_cycles = cycles;
   uint64_t total = 0;
-  double tk = 0, tcount = 0, tc_ = 0;
+  double tk = 0, tcount = 0;
   int64_t n_total = 0;
   for (int i = 0; i < p; ++i) n_total += ht[(size_t)i * p].rows;
   const int64_t NOBOUND = ((int64_t)1 << 31) - 1;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventRecord(e0, (cudaStream_t)o.stream);
   for (int i = 0; i < p && !rc; ++i)
     for (int j = 0; j < p && !rc; ++j)
       for (int k = 0; k < p && !rc; ++k) {
         const int A = i * p + j, Bt = i * p + k, C = k * p + j;
+        if (ht[A].rows == 0 || ht[A].m == 0 || ht[Bt].m == 0) continue;
         if ((rc = fetch(A, A, Bt, C)) || (rc = fetch(Bt, A, Bt, C)) || (rc = fetch(C, A, Bt, C))) break;
-        tc::DevGraph3 g{};
+        DevGraph3 g{};
         g.begA = dt[A].beg; g.adjA = dt[A].adj;
         g.begB = dt[Bt].beg; g.adjB = dt[Bt].adj;
         g.begC = dt[C].beg; g.adjC = dt[C].adj;
@@ -184,27 +175,107 @@ int trust_tc_count_partitioned(const char *folder, int parts, const trust_tc_opt
         g.min_deg = 1;
         trust_tc_result jr;
         memset(&jr, 0, sizeof jr);
-        if (g.rows == 0 || g.mA == 0 || g.mB == 0) continue;
-        rc = tc::count_device(&ctx, g, o, true, &jr);
+        rc = count_device(&ctx, g, o, true, &jr);
         total += jr.triangles;
+        r->wedges += jr.wedges;
         tk += jr.kernel_seconds;
         tcount += jr.count_seconds;
-        tc_ += jr.call_seconds;
         r->max_out_degree = std::max(r->max_out_degree, jr.max_out_degree);
         for (int c = 0; c < TC_NUM_CLASSES; ++c) r->class_sizes[c] += jr.class_sizes[c];
       }
+  cudaEventRecord(e1, (cudaStream_t)o.stream);
+  cudaEventSynchronize(e1);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
   for (auto &d : dt) {
     cudaFree(d.beg);
     cudaFree(d.adj);
   }
-  tc::ctx_release(&ctx);
-  free_host();
+  ctx_release(&ctx);
   r->triangles = total;
   r->kernel_seconds = tk;
   r->count_seconds = tcount;
-  r->call_seconds = tc_;
+  r->call_seconds = ms * 1e-3;
   r->vertices = n_total;
   r->edges = total_m;
+  (void)copied;
+  return rc;
+}
+
+}  // namespace tc
+
+extern "C" {
+
+int trust_tc_count_tiles_device(const int64_t *d_begin, const int32_t *d_adj, int64_t n, int64_t m, int parts,
+                                size_t device_budget_bytes, const trust_tc_opts *opts, trust_tc_result *r) {
+  if (!d_begin || (m > 0 && !d_adj) || n < 1 || m < 0 || n >= ((int64_t)1 << 31) || m >= ((int64_t)1 << 31) ||
+      !r || parts < 1 || parts > 32)
+    return TRUST_TC_E_ARG;
+  trust_tc_opts o;
+  if (opts) o = *opts; else trust_tc_opts_init(&o);
+  int rc = TRUST_TC_OK;
+  {  // validate the whole CSR before the partition reads it
+    trust_tc_ctx ctx;
+    rc = tc::ctx_init(&ctx, o.device);
+    if (!rc) {
+      cudaError_t e = cudaMemset(ctx.d_ctl, 0, sizeof(TcControl));
+      rc = e == cudaSuccess ? tc::launch_check(d_begin, d_adj, n, m, n, 1, ctx.d_ctl, ctx.num_sms, 0)
+                            : tc::cuda_status(e);
+      if (!rc) {
+        e = cudaMemcpy(ctx.h_ctl, ctx.d_ctl, sizeof(TcControl), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) rc = tc::cuda_status(e);
+      }
+      if (!rc) {
+        const int st = ctx.h_ctl->status;
+        if (st & TC_DEV_BAD_OFFSETS) rc = TRUST_TC_E_OFFSETS;
+        else if (st & TC_DEV_TOO_LARGE) rc = TRUST_TC_E_TOO_LARGE;
+        else if (st & TC_DEV_BAD_IDS) rc = TRUST_TC_E_IDS;
+      }
+    }
+    tc::ctx_release(&ctx);
+    if (rc) return rc;
+  }
+  const int p = parts;
+  std::vector<tc::PinnedTile> pt((size_t)p * p);
+  rc = tc::partition_device_to_host(d_begin, d_adj, n, m, p, pt.data());
+  if (rc) return rc;
+  std::vector<HostTile> ht((size_t)p * p);
+  for (size_t t = 0; t < pt.size(); ++t) {
+    ht[t].beg = pt[t].beg;
+    ht[t].adj = pt[t].adj;
+    ht[t].rows = pt[t].rows;
+    ht[t].m = pt[t].m;
+  }
+  rc = tc::tile_loop(ht, p, o, device_budget_bytes, r);
+  for (auto &t : pt) {
+    cudaFreeHost(t.beg);
+    cudaFreeHost(t.adj);
+  }
+  return rc;
+}
+
+int trust_tc_count_partitioned(const char *folder, int parts, const trust_tc_opts *opts, trust_tc_result *r) {
+  if (!folder || !r || parts < 1 || parts > 64) return TRUST_TC_E_ARG;
+  trust_tc_opts o;
+  if (opts) o = *opts; else trust_tc_opts_init(&o);
+  const int p = parts;
+  std::vector<HostTile> ht((size_t)p * p);
+  int rc = TRUST_TC_OK;
+  for (int i = 0; i < p && !rc; ++i)
+    for (int j = 0; j < p && !rc; ++j) {
+      HostTile &t = ht[(size_t)i * p + j];
+      rc = trust_tc_load_folder(tile_dir(folder, i, j).c_str(), &t.beg, &t.adj, &t.rows, &t.m);
+    }
+  for (int i = 0; i < p && !rc; ++i)
+    for (int j = 1; j < p && !rc; ++j)
+      if (ht[(size_t)i * p + j].rows != ht[(size_t)i * p].rows) rc = TRUST_TC_E_FORMAT;
+  if (!rc) rc = tc::tile_loop(ht, p, o, 0, r);
+  for (auto &t : ht) {
+    free(t.beg);
+    free(t.adj);
+  }
   return rc;
 }
 
