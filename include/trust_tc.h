@@ -78,6 +78,10 @@ typedef struct trust_tc_opts {
   int direction_split;   /* charge arcs with d(u) > d(v) to u's side (hash N+(u), stream N+(v)):
                             -1 = the learned schedule decides, 0 = never, 1 = always; applied only
                             when every row is strictly increasing (duplicate-free)             */
+  int hub_cluster;       /* rows above the CTA table (out-degree > 4096): 0 = in shared memory,
+                            one CTA while the table fits in 64 KiB, else a thread-block cluster
+                            with the table split over its CTAs (distributed shared memory);
+                            1/2/4/8 = that cluster size; -1 = per-CTA global tables          */
 } trust_tc_opts;
 
 typedef struct trust_tc_result {

@@ -79,6 +79,51 @@ def test_every_class_path(ctx, name, wm, bm):
     assert r.class_sizes["skip"] == int(np.sum(d < 2))
 
 
+@pytest.mark.parametrize("hub_cluster", [-1, 0, 1, 2, 4, 8])
+@pytest.mark.parametrize("name,bm", [("k150", 32), ("rmat_s12", 32), ("rmat_s12", 64), ("k60", 32)])
+def test_hub_rows_on_clusters(ctx, name, bm, hub_cluster):
+    """Rows above the CTA table counted in shared memory (one CTA or a thread-block cluster
+    whose CTAs share the table), or on per-CTA global tables (-1): the same count."""
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", name + ".npz"))
+    db, da = _dev(z["ref_beg"], z["ref_adj"])
+    r = T.count_csr(db, da, ctx=ctx, warp_max=32, block_max=bm, hub_cluster=hub_cluster)
+    assert r.triangles == int(z["nx_triangles"][0])
+    assert r.class_sizes["huge"] > 0
+
+
+@pytest.mark.parametrize("hub_cluster", [0, 1, 2, 4, 8, -1])
+def test_hub_row_larger_than_one_cta(ctx, hub_cluster):
+    """One row of 20,000 entries (a 65,536-slot table, 256 KiB: more than one CTA's shared
+    memory): the default spreads it over a 4-CTA cluster; a cluster too small for it falls back
+    to the global table.  Row 0 = 1..D, row i = {i+1}: the count is D - 1."""
+    D = 20_000
+    beg = np.concatenate([[0], D + np.arange(0, D + 1)]).astype(np.int64)
+    adj = np.concatenate([np.arange(1, D + 1), np.arange(2, D + 2)]).astype(np.int32)
+    adj[-1] = 0  # row D points back to 0 (keeps ids in range)
+    expect = O.count_forward(beg, adj)
+    assert expect == D - 1
+    r = T.count_csr(*_dev(beg, adj), ctx=ctx, hub_cluster=hub_cluster)
+    assert r.triangles == expect and r.class_sizes["huge"] == 1
+
+
+def test_hub_rows_on_clusters_split_and_record(ctx):
+    """Hub rows in shared memory in both passes of the direction split and with cycle recording."""
+    import torch
+    pairs = T.gen_rmat(16, 16, seed=1)
+    beg, adj = T.build_csr(pairs, 1 << 16)
+    expect = T.count_csr(beg, adj, ctx=ctx, hub_cluster=-1, warp_max=32, block_max=64).triangles
+    for hc in (0, 2, 8):
+        r = T.count_csr(beg, adj, ctx=ctx, warp_max=32, block_max=64, hub_cluster=hc, direction_split=1)
+        assert r.triangles == expect and r.direction_split
+        cyc = torch.zeros(beg.numel() - 1, dtype=torch.int64, device="cuda")
+        r = T.count_csr(beg, adj, ctx=ctx, warp_max=32, block_max=64, hub_cluster=hc, direction_split=0, cycles=cyc)
+        assert r.triangles == expect
+        d = np.diff(beg.cpu().numpy())
+        assert np.all(cyc.cpu().numpy()[d > 128] > 0)  # hub rows recorded too
+    with pytest.raises(T.TrustTcError):
+        T.count_csr(beg, adj, ctx=ctx, warp_max=32, block_max=64, hub_cluster=3)
+
+
 @pytest.mark.parametrize("threads", [64, 128, 256, 512, 1024])
 @pytest.mark.parametrize("blocks,chunk", [(0, 0), (1, 1), (7, 3), (300, 16)])
 def test_launch_shapes(ctx, threads, blocks, chunk):

@@ -113,7 +113,7 @@ def _is_torch_cuda(x) -> bool:
 
 def count_csr(beg, adj, *, ctx: Context | None = None, threads=0, blocks=0, chunk=0, stream=None,
               validate=VALIDATE_FULL, warp_max=0, block_max=0, schedule=SCHED_LEARNED,
-              cycles=None, direction_split=-1, model=None) -> CountResult:
+              cycles=None, direction_split=-1, model=None, hub_cluster=0) -> CountResult:
     """Count over a CSR held in numpy arrays (host) or contiguous torch CUDA tensors (device).
 
     `stream` is a cudaStream_t value (e.g. torch.cuda.current_stream().cuda_stream)."""
@@ -132,6 +132,7 @@ def count_csr(beg, adj, *, ctx: Context | None = None, threads=0, blocks=0, chun
         keep = (b, a)
     o = _opts(threads, blocks, chunk, kind, validate, warp_max, block_max, stream, schedule=schedule)
     o.direction_split = direction_split
+    o.hub_cluster = hub_cluster
     if model is not None:  # host float32 array of model_floats() entries (learned schedule)
         model = np.ascontiguousarray(model, dtype=np.float32)
         o.model = model.ctypes.data_as(C.c_void_p)

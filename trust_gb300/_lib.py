@@ -33,6 +33,7 @@ class Opts(C.Structure):
         ("stream", C.c_void_p),
         ("model", C.c_void_p),
         ("direction_split", C.c_int),
+        ("hub_cluster", C.c_int),
     ]
 
 

@@ -17,6 +17,8 @@
 #include <cstdio>
 #include <cstring>
 
+#include <cooperative_groups.h>
+
 #include "tc_count.h"
 
 namespace tc {
@@ -758,6 +760,11 @@ __global__ void __launch_bounds__(MAXT, MINB) count_kernel(CountArgs p) {
       const int t = bs.item;
       if (t >= n_items) break;
       const int v = list[t];
+      if (c == TC_CLASS_HUGE && p.hub_max_degree > 0) {  // counted by hub_kernel instead
+        int hb, hd;
+        row_of(p.begA, arow(p, v), hb, hd);
+        if (hd <= p.hub_max_degree) continue;
+      }
       const long long t_start = REC ? clock64() : 0;
       const unsigned long long h0 = hits;
       cta_vertex<SAME>(p, v, tab, bs, hits, wedges);
@@ -809,6 +816,134 @@ __global__ void __launch_bounds__(MAXT, MINB) count_kernel(CountArgs p) {
   __syncthreads();
   if (threadIdx.x == 0 && bs.count) atomicAdd(&p.ctl->count, bs.count);
   if (threadIdx.x == 0 && bs.wedges) atomicAdd(&p.ctl->wedges, bs.wedges);
+}
+
+// ------------------------------------------------------------------------------------------
+// hub rows in shared memory: one CTA, or a thread-block cluster (distributed shared memory)
+// ------------------------------------------------------------------------------------------
+// A hub row's table (2^log2 slots, as for a CTA table) is split evenly over the C CTAs of a
+// cluster: slot s lives in CTA s >> share_log2 at index s & (2^share_log2 - 1).  Inserts and
+// probes reach the other CTAs' slots through distributed shared memory; the cluster's warps claim
+// the hub's 32-arc batches from a counter in CTA 0's shared memory.  C = 1 is a single CTA with a
+// table larger than the persistent kernel's.
+namespace cg = cooperative_groups;
+
+struct DsmemSet {
+  int *local;
+  int log2;        // table slots: 2^log2
+  int share_log2;  // slots per CTA
+  __device__ __forceinline__ int *slot(unsigned s) const {
+    return cg::this_cluster().map_shared_rank(local, (int)(s >> share_log2)) + (s & ((1u << share_log2) - 1u));
+  }
+  __device__ __forceinline__ int has(int key) const {
+    const unsigned bmask = (1u << (log2 - 2)) - 1u;
+    unsigned b = tc_hash((unsigned)key, log2 - 2);
+    for (unsigned it = 0; it <= bmask; ++it) {
+      const int4 q = *reinterpret_cast<const int4 *>(slot(b << 2));
+      if (q.x == key || q.y == key || q.z == key || q.w == key) return 1;
+      if ((q.x | q.y | q.z | q.w) < 0) return 0;
+      b = (b + 1u) & bmask;
+    }
+    return 0;
+  }
+  __device__ __forceinline__ bool insert(int key) const {
+    const unsigned mask = (1u << log2) - 1u;
+    unsigned h = tc_hash((unsigned)key, log2 - 2) << 2;
+    for (unsigned it = 0; it <= mask; ++it) {
+      const int prev = atomicCAS(slot(h), -1, key);
+      if (prev == -1 || prev == key) return true;
+      h = (h + 1u) & mask;
+    }
+    return false;
+  }
+};
+
+// Persistent over the huge list: cluster k takes hubs k, k + clusters, ...; rows longer than
+// p.hub_max_degree are left to the main kernel's spill tables.  Every cluster.sync() is reached
+// by all CTAs of the cluster (the loop bounds and the skip test are the same for all of them);
+// no remote access happens before the first sync of a hub, and none after the final sync.
+template <bool SAME>
+__global__ void __launch_bounds__(512, 1) hub_kernel(CountArgs p, int log2C) {
+  extern __shared__ int smem[];
+  __shared__ int next_batch;
+  cg::cluster_group cl = cg::this_cluster();
+  const int C = 1 << log2C;
+  const int rank = (int)cl.block_rank();
+  const int lane = threadIdx.x & 31;
+  const int clusters = gridDim.x >> log2C;
+  const int cid = blockIdx.x >> log2C;
+  const int n_items = p.ctl->class_count[TC_CLASS_HUGE];
+  const int *list = class_list(p, TC_CLASS_HUGE);
+  int *ctr = cl.map_shared_rank(&next_batch, 0);
+  unsigned long long hits = 0, wedges = 0;
+  for (int t = cid; t < n_items; t += clusters) {
+    const int v = list[t];
+    int bA, dA, bB, dB;
+    row_of(p.begA, arow(p, v), bA, dA);
+    if (dA > p.hub_max_degree) continue;  // the same in every CTA of the cluster
+    if (SAME) { bB = bA; dB = dA; } else { row_of(p.begB, v, bB, dB); }
+    const long long t_start = p.cycles ? clock64() : 0;
+    const int log2 = ceil_log2_table(dA);
+    const DsmemSet set{smem, log2, log2 - log2C};
+    const int share = 1 << (log2 - log2C);
+    for (int i = threadIdx.x; i < share; i += blockDim.x) smem[i] = -1;
+    if (rank == 0 && threadIdx.x == 0) next_batch = 0;
+    cl.sync();
+    bool ok = true;
+    for (int i = rank * blockDim.x + threadIdx.x; i < dA; i += C * blockDim.x)
+      ok &= set.insert(tc_ld_nc(p.adjA + bA + i));
+    if (!ok) atomicOr(&p.ctl->status, TC_DEV_TABLE_FULL);
+    cl.sync();
+    const int nbatch = (dB + 31) >> 5;
+    for (;;) {
+      int bt = 0;
+      if (lane == 0) bt = atomicAdd(ctr, 1);
+      bt = __shfl_sync(TC_FULL_MASK, bt, 0);
+      if (bt >= nbatch) break;
+      const int i = (bt << 5) + lane;
+      int s = 0, dd = 0;
+      if (i < dB) row_of(p.begC, tc_ld_nc(p.adjB + bB + i), s, dd);
+      if (SAME && p.split && dd > dB) dd = 0;
+      probe_arcs<32, LongRow<32>::value>(p.adjC, s, dd, lane, set, hits, wedges);
+    }
+    cl.sync();  // every probe of this hub is done before any share is cleared again
+    if (p.cycles && rank == 0 && threadIdx.x == 0) p.cycles[v] = (unsigned long long)(clock64() - t_start);
+  }
+  cl.sync();  // no CTA leaves while another may still read its shared memory
+#pragma unroll
+  for (int off = 16; off >= 1; off >>= 1) {
+    hits += __shfl_down_sync(TC_FULL_MASK, hits, off);
+    wedges += __shfl_down_sync(TC_FULL_MASK, wedges, off);
+  }
+  if (lane == 0 && hits) atomicAdd(&p.ctl->count, hits);
+  if (lane == 0 && wedges) atomicAdd(&p.ctl->wedges, wedges);
+}
+
+int launch_hub(bool same, const CountArgs &a, int max_log2, int log2C, int clusters, cudaStream_t st) {
+  const size_t smem = (size_t)4 << (max_log2 - log2C);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)(clusters << log2C));
+  cfg.blockDim = dim3(512);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = 1u << log2C;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaError_t e;
+  if (same) {
+    e = cudaFuncSetAttribute(hub_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess) e = cudaLaunchKernelEx(&cfg, hub_kernel<true>, a, log2C);
+  } else {
+    e = cudaFuncSetAttribute(hub_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess) e = cudaLaunchKernelEx(&cfg, hub_kernel<false>, a, log2C);
+  }
+  TC_CUDA_TRY(e);
+  TC_NOTE_LAUNCH();
+  return TRUST_TC_OK;
 }
 
 // ------------------------------------------------------------------------------------------

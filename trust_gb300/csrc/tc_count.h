@@ -34,6 +34,8 @@ struct CountArgs {
   const int *graph_of;
   unsigned long long *graph_counts;
   int dev_off;
+  // huge rows up to this out-degree are counted by hub_kernel in shared memory (0: none)
+  int hub_max_degree;
 };
 
 int launch_check(const int64_t *beg, const int32_t *adj, int64_t rows, int64_t m, int64_t id_bound,
@@ -52,6 +54,9 @@ int launch_batch_classify(int pass, const int64_t *beg, int64_t rows, const int 
                           const unsigned char *graph_sc, const BatchThresholds &th, TcControl *ctl, int *lists,
                           int num_sms, cudaStream_t st);
 int launch_batch_offsets(TcControl *ctl, int nsc, cudaStream_t st);
+// Hub rows (huge class, out-degree <= a.hub_max_degree) on clusters of 2^log2C CTAs of 512
+// threads; tables up to 2^max_log2 slots, 2^(max_log2 - log2C) per CTA in shared memory.
+int launch_hub(bool same, const CountArgs &a, int max_log2, int log2C, int clusters, cudaStream_t st);
 int count_kernel_occupancy(bool same, int threads, size_t smem_bytes, int *blocks_per_sm);
 // Shared-memory carveout hint: just enough for `per_sm` resident CTAs of `smem_bytes` each.
 int set_count_kernel_carveout(bool same, int threads, size_t smem_bytes, int per_sm);

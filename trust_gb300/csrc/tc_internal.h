@@ -74,6 +74,7 @@ struct DevGraph3 {
   int64_t mA, mB, mC;         // entries of each
   int64_t boundA, boundB, boundC;  // exclusive id bound per CSR (B's ids index rows of C)
   int min_deg;                // rows with fewer entries in A or B are skipped
+  int64_t max_deg_A;          // largest row of A when known (0: the validation pass's maximum)
 };
 
 int ctx_init(trust_tc_ctx *c, int device);
