@@ -490,6 +490,11 @@ __device__ __forceinline__ void row_of(const int64_t *__restrict__ beg, int v, i
 __device__ __forceinline__ const int *class_list(const CountArgs &p, int c) {
   return p.lists + (p.dev_off ? p.ctl->class_off[c] : p.off.off[c]);
 }
+template <bool BATCH>
+__device__ __forceinline__ const int *class_list_t(const CountArgs &p, int c) {
+  if constexpr (BATCH) return p.lists + p.ctl->class_off[c];
+  else return p.lists + p.off.off[c];
+}
 
 // Per-graph attribution of a batch.  Every lane keeps the hits of the graph its warp is
 // currently working on; when the warp moves to another graph the warp's sum goes to that graph's
@@ -642,7 +647,9 @@ struct GroupStage {
 // Drain one group class.  Each warp claims `chunk` steps of 32/G vertices.  Loads run three
 // steps ahead: while step t is probed, step t+1's target rows, step t+2's row elements and
 // step t+3's row bounds are in flight (the reference walks this chain serially per vertex).
-template <int G, bool SAME, bool REC>
+// BATCH: the batch instantiation (per-graph attribution, device list offsets); the single-graph
+// kernel carries none of its state.
+template <int G, bool SAME, bool REC, bool BATCH>
 __device__ void drain_group_class(const CountArgs &p, int c, int *warp_tab, unsigned long long &hits,
                                   unsigned long long &wedges, BatchAcc &acc) {
   constexpr int GPW = 32 / G;
@@ -650,7 +657,7 @@ __device__ void drain_group_class(const CountArgs &p, int c, int *warp_tab, unsi
   const int g = lane / G;
   const int glane = lane & (G - 1);
   const int n_items = p.ctl->class_count[c];
-  const int *list = class_list(p, c);
+  const int *list = class_list_t<BATCH>(p, c);
   const int claim = p.chunk * GPW;
   // stage loaders
   auto ld_v = [&](int item, int t1) { return item < t1 ? list[item] : -1; };
@@ -696,7 +703,7 @@ __device__ void drain_group_class(const CountArgs &p, int c, int *warp_tab, unsi
       ld_elem(s2);
       ld_row(s3);
       const long long t_start = REC ? clock64() : 0;
-      if (!p.graph_of) {
+      if constexpr (!BATCH) {
         group_vertex<G, SAME>(p, s0.uA, s0.s, s0.dd, warp_tab, hits, wedges);
       } else {
         // a batch: one pass per graph present in this step (almost always one), the other
@@ -735,7 +742,7 @@ __device__ void drain_group_class(const CountArgs &p, int c, int *warp_tab, unsi
 // with at least TC_MIN_CTAS_256 CTAs resident per SM (the default shape).
 constexpr int TC_MIN_CTAS_256 = 5;
 
-template <bool SAME, bool REC, int MAXT, int MINB>
+template <bool SAME, bool REC, int MAXT, int MINB, bool BATCH>
 __global__ void __launch_bounds__(MAXT, MINB) count_kernel(CountArgs p) {
   extern __shared__ int smem[];
   __shared__ BlockShared bs;
@@ -750,7 +757,7 @@ __global__ void __launch_bounds__(MAXT, MINB) count_kernel(CountArgs p) {
     const int n_items = p.ctl->class_count[c];
     if (n_items == 0) continue;
     if (c == TC_CLASS_HUGE && (int)blockIdx.x >= p.huge_blocks) continue;
-    const int *list = class_list(p, c);
+    const int *list = class_list_t<BATCH>(p, c);
     int *tab = (c == TC_CLASS_HUGE) ? p.huge_tables + (size_t)blockIdx.x * ((size_t)1 << p.huge_log2)
                                     : smem;
     for (;;) {
@@ -769,7 +776,7 @@ __global__ void __launch_bounds__(MAXT, MINB) count_kernel(CountArgs p) {
       const unsigned long long h0 = hits;
       cta_vertex<SAME>(p, v, tab, bs, hits, wedges);
       if (REC && threadIdx.x == 0) p.cycles[v] = (unsigned long long)(clock64() - t_start);
-      if (p.graph_of) batch_take(p, acc, p.graph_of[v], hits - h0);
+      if constexpr (BATCH) batch_take(p, acc, p.graph_of[v], hits - h0);
     }
   }
   __syncthreads();
@@ -779,7 +786,7 @@ __global__ void __launch_bounds__(MAXT, MINB) count_kernel(CountArgs p) {
   {
     const int c = TC_CLASS_WARP;
     const int n_items = p.ctl->class_count[c];
-    const int *list = class_list(p, c);
+    const int *list = class_list_t<BATCH>(p, c);
     for (;;) {
       int t0 = 0;
       // warp-class vertices are large: claim them one at a time unless the chunk is very coarse
@@ -794,15 +801,15 @@ __global__ void __launch_bounds__(MAXT, MINB) count_kernel(CountArgs p) {
         const unsigned long long h0 = hits;
         warp_vertex<SAME>(p, v, warp_tab, hits, wedges);
         if (REC && lane == 0) p.cycles[v] = (unsigned long long)(clock64() - t_start);
-        if (p.graph_of) batch_take(p, acc, p.graph_of[v], hits - h0);
+        if constexpr (BATCH) batch_take(p, acc, p.graph_of[v], hits - h0);
       }
     }
   }
-  drain_group_class<32, SAME, REC>(p, TC_CLASS_G32, warp_tab, hits, wedges, acc);
-  drain_group_class<16, SAME, REC>(p, TC_CLASS_G16, warp_tab, hits, wedges, acc);
-  drain_group_class<8, SAME, REC>(p, TC_CLASS_G8, warp_tab, hits, wedges, acc);
-  drain_group_class<4, SAME, REC>(p, TC_CLASS_G4, warp_tab, hits, wedges, acc);
-  if (p.graph_of) batch_flush(p, acc);
+  drain_group_class<32, SAME, REC, BATCH>(p, TC_CLASS_G32, warp_tab, hits, wedges, acc);
+  drain_group_class<16, SAME, REC, BATCH>(p, TC_CLASS_G16, warp_tab, hits, wedges, acc);
+  drain_group_class<8, SAME, REC, BATCH>(p, TC_CLASS_G8, warp_tab, hits, wedges, acc);
+  drain_group_class<4, SAME, REC, BATCH>(p, TC_CLASS_G4, warp_tab, hits, wedges, acc);
+  if constexpr (BATCH) batch_flush(p, acc);
 
   // Reduction: warp shuffle -> shared u64 -> one global u64 atomic per CTA
   // (the reference does per-thread shared atomics, Without-graph-partition/TC.cu:586-599).
@@ -983,13 +990,14 @@ int launch_classify(int pass, const int64_t *begA, const int64_t *begB, int64_t 
 template <bool SAME, int MAXT, int MINB>
 static cudaError_t occupancy_of(int threads, size_t smem_bytes, int *blocks_per_sm) {
   cudaError_t e = cudaSuccess;
-  for (auto fn : {count_kernel<SAME, false, MAXT, MINB>, count_kernel<SAME, true, MAXT, MINB>}) {
+  for (auto fn : {count_kernel<SAME, false, MAXT, MINB, false>, count_kernel<SAME, true, MAXT, MINB, false>,
+                  count_kernel<SAME, false, MAXT, MINB, SAME>}) {
     if (e == cudaSuccess) e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
     if (e == cudaSuccess)
       e = cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
   }
   if (e == cudaSuccess)
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, count_kernel<SAME, false, MAXT, MINB>, threads,
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, count_kernel<SAME, false, MAXT, MINB, false>, threads,
                                                       smem_bytes);
   return e;
 }
@@ -1008,10 +1016,10 @@ int count_kernel_occupancy(bool same, int threads, size_t smem_bytes, int *block
 
 template <bool SAME, int MAXT, int MINB>
 static cudaError_t carveout_of(int pct) {
-  cudaError_t e = cudaFuncSetAttribute(count_kernel<SAME, false, MAXT, MINB>,
-                                       cudaFuncAttributePreferredSharedMemoryCarveout, pct);
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(count_kernel<SAME, true, MAXT, MINB>, cudaFuncAttributePreferredSharedMemoryCarveout, pct);
+  cudaError_t e = cudaSuccess;
+  for (auto fn : {count_kernel<SAME, false, MAXT, MINB, false>, count_kernel<SAME, true, MAXT, MINB, false>,
+                  count_kernel<SAME, false, MAXT, MINB, SAME>})
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, pct);
   return e;
 }
 
@@ -1031,10 +1039,12 @@ int set_count_kernel_carveout(bool same, int threads, size_t smem_bytes, int per
 
 template <bool SAME, int MAXT, int MINB>
 static void launch_one(const CountArgs &a, int blocks, int threads, size_t smem_bytes, cudaStream_t st) {
-  if (a.cycles)
-    count_kernel<SAME, true, MAXT, MINB><<<blocks, threads, smem_bytes, st>>>(a);
+  if (SAME && a.graph_of)  // batches: one graph CSR, no cycle recording
+    count_kernel<SAME, false, MAXT, MINB, SAME><<<blocks, threads, smem_bytes, st>>>(a);
+  else if (a.cycles)
+    count_kernel<SAME, true, MAXT, MINB, false><<<blocks, threads, smem_bytes, st>>>(a);
   else
-    count_kernel<SAME, false, MAXT, MINB><<<blocks, threads, smem_bytes, st>>>(a);
+    count_kernel<SAME, false, MAXT, MINB, false><<<blocks, threads, smem_bytes, st>>>(a);
   TC_NOTE_LAUNCH();
 }
 
