@@ -312,13 +312,15 @@ int trust_tc_batch_create(trust_tc_ctx *ctx, const int64_t *d_begin, const int32
   if ((rc = cu(cudaMallocHost((void **)&b->h_counts, sizeof(unsigned long long) * G)))) return fail(rc);
   if ((rc = cu(cudaMalloc((void **)&b->d_ctl, sizeof(TcControl) * TC_BATCH_CLASSES)))) return fail(rc);
   if ((rc = cu(cudaMallocHost((void **)&b->h_ctl, sizeof(TcControl) * TC_BATCH_CLASSES)))) return fail(rc);
+  memset(b->h_ctl, 0, sizeof(TcControl) * TC_BATCH_CLASSES);
   if ((rc = cu(cudaMalloc((void **)&b->d_lists, sizeof(int) * (size_t)n)))) return fail(rc);
   if ((rc = cu(cudaMemcpy(b->d_vbeg, graph_vbeg, sizeof(int64_t) * (G + 1), cudaMemcpyHostToDevice)))) return fail(rc);
   if ((rc = cu(cudaMemcpy(b->d_graph_sc, sc.data(), G, cudaMemcpyHostToDevice)))) return fail(rc);
   // validation of the union (offsets, ids, row lengths), then graph ids and the per-class scan
   if ((rc = cu(cudaMemsetAsync(b->d_ctl, 0, sizeof(TcControl) * TC_BATCH_CLASSES, b->st)))) return fail(rc);
   if ((rc = launch_check(d_begin, d_adj, n, m, n, 1, b->d_ctl, ctx->num_sms, b->st))) return fail(rc);
-  if ((rc = cu(cudaMemcpyAsync(b->h_ctl, b->d_ctl, sizeof(TcControl), cudaMemcpyDeviceToHost, b->st))))
+  if ((rc = cu(cudaMemcpyAsync(b->h_ctl, b->d_ctl, sizeof(TcControl) * TC_BATCH_CLASSES, cudaMemcpyDeviceToHost,
+                               b->st))))
     return fail(rc);
   if ((rc = cu(cudaStreamSynchronize(b->st)))) return fail(rc);
   if ((rc = batch_status(b))) return fail(rc);
