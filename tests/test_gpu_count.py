@@ -106,6 +106,22 @@ def test_hub_row_larger_than_one_cta(ctx, hub_cluster):
     assert r.triangles == expect and r.class_sizes["huge"] == 1
 
 
+def test_hub_row_unaligned_neighbour_array(ctx):
+    """Hub rows are staged into shared memory by TMA bulk copies of their 16-byte aligned interior;
+    a neighbour array that is not 16-byte aligned (a view one element in) is read directly."""
+    import torch
+    D = 20_000
+    beg = np.concatenate([[0], D + np.arange(0, D + 1)]).astype(np.int64)
+    adj = np.concatenate([np.arange(1, D + 1), np.arange(2, D + 2)]).astype(np.int32)
+    adj[-1] = 0
+    db = torch.from_numpy(beg).cuda()
+    big = torch.zeros(adj.size + 1, dtype=torch.int32, device="cuda")
+    big[1:] = torch.from_numpy(adj).cuda()
+    for hc in (0, 1, 4):
+        assert T.count_csr(db, big[1:], ctx=ctx, hub_cluster=hc).triangles == D - 1
+        assert T.count_csr(db, big[1:].clone(), ctx=ctx, hub_cluster=hc).triangles == D - 1
+
+
 def test_hub_rows_on_clusters_split_and_record(ctx):
     """Hub rows in shared memory in both passes of the direction split and with cycle recording."""
     import torch

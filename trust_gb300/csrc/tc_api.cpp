@@ -291,7 +291,8 @@ int count_device(trust_tc_ctx *c, const DevGraph3 &g, const trust_tc_opts &o, bo
     } else {
       hub_log2C = std::min(std::max(tlog2 - 14, 0), 3);
     }
-    const int share_cap_log2 = ceil_log2_size((int64_t)(c->max_smem_optin - 1024) / 4 + 1) - 1;
+    // the share and a staging buffer of half its size must fit one CTA's opt-in shared memory
+    const int share_cap_log2 = ceil_log2_size((int64_t)(c->max_smem_optin - 2048) * 2 / 3 / 4 + 1) - 1;
     hub_max_log2 = std::min(tlog2, share_cap_log2 + hub_log2C);
     hub_log2C = std::min(hub_log2C, hub_max_log2 - 3);  // at least 8 slots per CTA
     a.hub_max_degree = 1 << (hub_max_log2 - 1);
@@ -366,7 +367,7 @@ int count_device(trust_tc_ctx *c, const DevGraph3 &g, const trust_tc_opts &o, bo
   TC_CUDA_TRY(cudaEventRecord(c->ev[4], st));
   TC_CUDA_TRY(cudaStreamSynchronize(st));
   const TcControl done = *c->h_ctl;
-  if (done.status & TC_DEV_TABLE_FULL) return TRUST_TC_E_DEVICE;
+  if (done.status & (TC_DEV_TABLE_FULL | TC_DEV_WAIT_LIMIT)) return TRUST_TC_E_DEVICE;
   float t_kernel = 0, t_count = 0, t_call = 0;
   TC_CUDA_TRY(cudaEventElapsedTime(&t_kernel, c->ev[1], c->ev[3]));
   TC_CUDA_TRY(cudaEventElapsedTime(&t_count, c->ev[2], c->ev[3]));

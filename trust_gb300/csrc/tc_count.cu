@@ -865,14 +865,62 @@ struct DsmemSet {
   }
 };
 
+// ---- TMA bulk copy (cp.async.bulk) into shared memory, completion on an mbarrier ----
+__device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned long long *bar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// One thread: arm the barrier for `bytes` and start the copy of [src, src + bytes) to dst.
+// src and dst 16-byte aligned, bytes a multiple of 16 (< 2^20).
+// The fence orders this CTA's earlier generic-proxy reads of dst before the copy's writes.
+__device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, unsigned bytes, unsigned long long *bar) {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+
+// Wait for the barrier's phase `parity` to complete, giving up after about a second of clock64
+// cycles (returns false then; the caller records TC_DEV_WAIT_LIMIT and stops using the copies).
+__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned parity) {
+  const long long t0 = clock64();
+  for (;;) {
+    unsigned done = 0;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if (clock64() - t0 > (2ll << 30)) return false;
+  }
+}
+
 // Persistent over the huge list: cluster k takes hubs k, k + clusters, ...; rows longer than
 // p.hub_max_degree are left to the main kernel's spill tables.  Every cluster.sync() is reached
 // by all CTAs of the cluster (the loop bounds and the skip test are the same for all of them);
 // no remote access happens before the first sync of a hub, and none after the final sync.
+// Each CTA stages its contiguous share of the hub row with one TMA bulk copy (the 16-byte aligned
+// interior; the ragged ends, at most 3 entries each, by plain loads) and inserts from shared
+// memory.  Dynamic shared memory: the table share (2^share_log2_max ints) then the staging buffer.
 template <bool SAME>
-__global__ void __launch_bounds__(512, 1) hub_kernel(CountArgs p, int log2C) {
-  extern __shared__ int smem[];
+__global__ void __launch_bounds__(512, 1) hub_kernel(CountArgs p, int log2C, int share_log2_max) {
+  extern __shared__ __align__(16) int smem[];
   __shared__ int next_batch;
+  __shared__ __align__(8) unsigned long long bar;
+  __shared__ int tma_ok;
+  int *stage = smem + (1 << share_log2_max);
+  if (threadIdx.x == 0) {
+    mbar_init(&bar);
+    tma_ok = ((reinterpret_cast<uintptr_t>(p.adjA) & 15) == 0);  // 16-byte aligned base: copy the interior
+  }
+  __syncthreads();
+  unsigned parity = 0;
   cg::cluster_group cl = cg::this_cluster();
   const int C = 1 << log2C;
   const int rank = (int)cl.block_rank();
@@ -897,8 +945,30 @@ __global__ void __launch_bounds__(512, 1) hub_kernel(CountArgs p, int log2C) {
     if (rank == 0 && threadIdx.x == 0) next_batch = 0;
     cl.sync();
     bool ok = true;
-    for (int i = rank * blockDim.x + threadIdx.x; i < dA; i += C * blockDim.x)
-      ok &= set.insert(tc_ld_nc(p.adjA + bA + i));
+    {  // this CTA's share of the row: entries [lo, hi)
+      const int per = (dA + C - 1) >> log2C;
+      const int lo = min(rank * per, dA), hi = min(lo + per, dA);
+      const long long a0 = (long long)bA + lo, a1 = (long long)bA + hi;
+      const long long i0 = (a0 + 3) & ~3ll, i1 = a1 & ~3ll;  // aligned interior [i0, i1)
+      if (tma_ok && i1 > i0) {
+        if (threadIdx.x == 0) bulk_copy_g2s(stage, p.adjA + i0, (unsigned)(i1 - i0) * 4u, &bar);
+        for (long long i = a0 + threadIdx.x; i < i0; i += blockDim.x) ok &= set.insert(tc_ld_nc(p.adjA + i));
+        for (long long i = i1 + threadIdx.x; i < a1; i += blockDim.x) ok &= set.insert(tc_ld_nc(p.adjA + i));
+        const bool arrived = mbar_wait(&bar, parity);
+        parity ^= 1u;
+        if (arrived) {
+          for (int i = threadIdx.x; i < (int)(i1 - i0); i += blockDim.x) ok &= set.insert(stage[i]);
+        } else {  // give up on the copy: report it and read the interior directly
+          if (threadIdx.x == 0) atomicOr(&p.ctl->status, TC_DEV_WAIT_LIMIT);
+          for (long long i = i0 + threadIdx.x; i < i1; i += blockDim.x) ok &= set.insert(tc_ld_nc(p.adjA + i));
+        }
+        __syncthreads();  // the staging buffer is free again, and every thread saw the same outcome
+        if (threadIdx.x == 0 && !arrived) tma_ok = 0;
+        __syncthreads();
+      } else {
+        for (long long i = a0 + threadIdx.x; i < a1; i += blockDim.x) ok &= set.insert(tc_ld_nc(p.adjA + i));
+      }
+    }
     if (!ok) atomicOr(&p.ctl->status, TC_DEV_TABLE_FULL);
     cl.sync();
     const int nbatch = (dB + 31) >> 5;
@@ -927,7 +997,10 @@ __global__ void __launch_bounds__(512, 1) hub_kernel(CountArgs p, int log2C) {
 }
 
 int launch_hub(bool same, const CountArgs &a, int max_log2, int log2C, int clusters, cudaStream_t st) {
-  const size_t smem = (size_t)4 << (max_log2 - log2C);
+  // table share + staging for one CTA's share of the longest row (plus alignment slack)
+  const int share_log2 = max_log2 - log2C;
+  const size_t stage_ints = (((size_t)a.hub_max_degree + (1u << log2C) - 1) >> log2C) + 8;
+  const size_t smem = ((size_t)4 << share_log2) + 4 * stage_ints;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)(clusters << log2C));
   cfg.blockDim = dim3(512);
@@ -943,10 +1016,10 @@ int launch_hub(bool same, const CountArgs &a, int max_log2, int log2C, int clust
   cudaError_t e;
   if (same) {
     e = cudaFuncSetAttribute(hub_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e == cudaSuccess) e = cudaLaunchKernelEx(&cfg, hub_kernel<true>, a, log2C);
+    if (e == cudaSuccess) e = cudaLaunchKernelEx(&cfg, hub_kernel<true>, a, log2C, share_log2);
   } else {
     e = cudaFuncSetAttribute(hub_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e == cudaSuccess) e = cudaLaunchKernelEx(&cfg, hub_kernel<false>, a, log2C);
+    if (e == cudaSuccess) e = cudaLaunchKernelEx(&cfg, hub_kernel<false>, a, log2C, share_log2);
   }
   TC_CUDA_TRY(e);
   TC_NOTE_LAUNCH();
