@@ -315,7 +315,8 @@ def run_ours(args, ws, rank, local):
                    "schedule": "learned (library default)", "class_sizes": res[0].class_sizes,
                    "parallelism": f"replicas x{ws}",
                    "l2": f"{L2_FLUSH_BYTES >> 20} MiB buffer written before every timed step (graph "
-                         f"{(8 * (n + 1) + 4 * m) / 1e6:.0f} MB fits in L2)"},
+                         f"{(8 * (n + 1) + 4 * m) / 1e6:.0f} MB"
+                         + (", fits in L2)" if 8 * (n + 1) + 4 * m < 126e6 else ", larger than L2)")},
         "schedules": sched,
         "learned_vs_plain": sched["learned"]["gteps"] / sched["plain"]["gteps"],
         "counts_consistent": ok,
