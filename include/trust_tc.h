@@ -225,6 +225,16 @@ double trust_tc_chung_lu_table(int64_t n, double gamma, double w_max, int64_t ta
 int trust_tc_gen_er_device(trust_tc_ctx *ctx, int64_t n, int64_t npairs, uint64_t seed,
                            int32_t *d_pairs);
 
+/* Autotuner for one graph (device CSR, opts->ptr_kind = TRUST_TC_DEVICE): times the counting call
+ * `repeats` times per candidate and keeps the fastest, by coordinate descent from `base` over
+ * threads per CTA (128/256/512/1024), warp-class bound (64/128/256), queue chunk (4/8/16) and, when
+ * the graph has rows above the CTA table, hub_cluster (0/1/2/4/-1).  *best receives the chosen
+ * options (pass them to trust_tc_count_csr), *best_ms their median call time.  Every candidate
+ * must give the same count (else TRUST_TC_E_DEVICE).  No counterpart in the reference, whose
+ * threads/blocks/chunk come from argv (Without-graph-partition/mpi_main.cpp:84-88). */
+int trust_tc_autotune(trust_tc_ctx *ctx, const int64_t *begin, const int32_t *adj, int64_t n, int64_t m,
+                      const trust_tc_opts *base, int repeats, trust_tc_opts *best, double *best_ms);
+
 /* ---- batches: many graphs counted by one CUDA-graph launch -------------------------------
  * A batch is the disjoint union of many oriented graphs in one device CSR (ids global), graph g
  * owning rows [graph_vbeg[g], graph_vbeg[g+1]) and no arc leaving its graph (build it with

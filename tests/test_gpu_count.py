@@ -122,6 +122,26 @@ def test_hub_row_unaligned_neighbour_array(ctx):
         assert T.count_csr(db, big[1:].clone(), ctx=ctx, hub_cluster=hc).triangles == D - 1
 
 
+def test_autotune(ctx):
+    """The autotuner returns valid launch parameters; they change the schedule, never the count."""
+    pairs = T.gen_rmat(16, 16, seed=1)
+    beg, adj = T.build_csr(pairs, 1 << 16)
+    expect = T.count_csr(beg, adj, ctx=ctx).triangles
+    cfg, ms = T.autotune(beg, adj, ctx, repeats=2)
+    assert ms > 0 and cfg["threads"] in (0, 128, 256, 512, 1024) and cfg["chunk"] in (0, 4, 8, 16)
+    assert T.count_csr(beg, adj, ctx=ctx, **cfg).triangles == expect
+    # a graph with a row above the CTA table: the hub cluster size is tuned too
+    import torch
+    D = 20_000
+    hb = torch.from_numpy(np.concatenate([[0], D + np.arange(0, D + 1)]).astype(np.int64)).cuda()
+    ha = np.concatenate([np.arange(1, D + 1), np.arange(2, D + 2)]).astype(np.int32)
+    ha[-1] = 0
+    ha = torch.from_numpy(ha).cuda()
+    cfg, ms = T.autotune(hb, ha, ctx, repeats=1)
+    assert cfg["hub_cluster"] in (0, 1, 2, 4, -1)
+    assert T.count_csr(hb, ha, ctx=ctx, **cfg).triangles == D - 1
+
+
 def test_hub_rows_on_clusters_split_and_record(ctx):
     """Hub rows in shared memory in both passes of the direction split and with cycle recording."""
     import torch

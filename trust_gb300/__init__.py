@@ -26,7 +26,7 @@ from ._lib import (CLASS_NAMES, DEVICE, HOST, SCHED_LEARNED, SCHED_PLAIN, SCHED_
 
 __all__ = [
     "arguments", "Triangle_count", "Context", "CountResult", "count_csr", "count_folder", "count_partitioned",
-    "count_tiles",
+    "count_tiles", "autotune",
     "load_folder", "save_folder", "partition_folder", "gen_rmat", "gen_chung_lu", "gen_er", "build_csr",
     "chung_lu_table", "gen_ba", "TrustTcError", "load", "model_floats", "model_init", "model_default", "model_grad",
     "model_train", "model_predict", "vertex_features",
@@ -160,6 +160,18 @@ def count_partitioned(folder: str, parts: int, threads=0, blocks=0, chunk=0) -> 
     check(load().trust_tc_count_partitioned(folder.encode(), parts, C.byref(o), C.byref(r)),
           "trust_tc_count_partitioned")
     return _result(r)
+
+
+def autotune(beg, adj, ctx: Context, repeats: int = 3, schedule=SCHED_LEARNED) -> tuple[dict, float]:
+    """Fastest launch parameters for this device CSR (torch CUDA tensors): (count_csr keyword
+    arguments, median call ms)."""
+    o = _opts(ptr_kind=DEVICE, schedule=schedule)
+    best = _lib.Opts()
+    ms = C.c_double()
+    check(load().trust_tc_autotune(ctx.handle, C.c_void_p(beg.data_ptr()), C.c_void_p(adj.data_ptr()), beg.numel() - 1,
+                                   adj.numel(), C.byref(o), repeats, C.byref(best), C.byref(ms)), "trust_tc_autotune")
+    return ({"threads": best.threads_per_block, "warp_max": best.warp_max_degree, "chunk": best.chunk,
+             "hub_cluster": best.hub_cluster, "schedule": best.schedule}, ms.value)
 
 
 def count_tiles(beg, adj, parts: int, budget_bytes: int = 0, threads=0, blocks=0, chunk=0,

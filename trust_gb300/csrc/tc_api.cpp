@@ -16,6 +16,7 @@
 #include <algorithm>
 #include <atomic>
 #include <string>
+#include <vector>
 
 #include "tc_count.h"
 #include "tc_internal.h"
@@ -498,6 +499,62 @@ int trust_tc_validate_csr(const int64_t *beg, const int32_t *adj, int64_t n, int
   for (int64_t i = 0; i < m; ++i)
     if (adj[i] < 0 || (int64_t)adj[i] >= n) return TRUST_TC_E_IDS;
   if (max_out_degree) *max_out_degree = dmax;
+  return TRUST_TC_OK;
+}
+
+int trust_tc_autotune(trust_tc_ctx *ctx, const int64_t *beg, const int32_t *adj, int64_t n, int64_t m,
+                      const trust_tc_opts *base, int repeats, trust_tc_opts *best, double *best_ms) {
+  if (!ctx || !best || repeats < 1) return TRUST_TC_E_ARG;
+  trust_tc_opts o;
+  if (base) o = *base; else trust_tc_opts_init(&o);
+  if (o.ptr_kind != TRUST_TC_DEVICE || o.record_cycles) return TRUST_TC_E_ARG;
+  // median call time of `repeats` calls under `t`; the first call's result checks the count
+  uint64_t expect = 0;
+  bool have = false;
+  int64_t huge = 0;
+  auto time_of = [&](const trust_tc_opts &t, double *ms) -> int {
+    std::vector<double> v;
+    for (int k = 0; k < repeats; ++k) {
+      trust_tc_result r;
+      memset(&r, 0, sizeof r);
+      int rc = trust_tc_count_csr(ctx, beg, adj, n, m, &t, &r);
+      if (rc) return rc;
+      if (have && r.triangles != expect) return TRUST_TC_E_DEVICE;  // a schedule never changes the count
+      expect = r.triangles;
+      have = true;
+      huge = r.class_sizes[TC_CLASS_HUGE];
+      v.push_back(r.call_seconds * 1e3);
+    }
+    std::sort(v.begin(), v.end());
+    *ms = v[v.size() / 2];
+    return TRUST_TC_OK;
+  };
+  double cur = 0;
+  int rc = time_of(o, &cur);
+  if (rc) return rc;
+  // coordinate descent over the launch parameters, each from the best so far
+  auto sweep = [&](int trust_tc_opts::*field, std::initializer_list<int> values) -> int {
+    for (int val : values) {
+      if (o.*field == val) continue;
+      trust_tc_opts t = o;
+      t.*field = val;
+      double ms = 0;
+      int e = time_of(t, &ms);
+      if (e == TRUST_TC_E_ARG) continue;  // not a valid combination (e.g. CTA bound below the warp bound)
+      if (e) return e;
+      if (ms < cur) {
+        cur = ms;
+        o = t;
+      }
+    }
+    return TRUST_TC_OK;
+  };
+  if ((rc = sweep(&trust_tc_opts::threads_per_block, {128, 256, 512, 1024}))) return rc;
+  if ((rc = sweep(&trust_tc_opts::warp_max_degree, {64, 128, 256}))) return rc;
+  if ((rc = sweep(&trust_tc_opts::chunk, {4, 8, 16}))) return rc;
+  if (huge > 0 && (rc = sweep(&trust_tc_opts::hub_cluster, {0, 1, 2, 4, -1}))) return rc;
+  *best = o;
+  if (best_ms) *best_ms = cur;
   return TRUST_TC_OK;
 }
 
