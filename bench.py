@@ -129,6 +129,22 @@ class ClockSampler:
                 "samples": len(rows), "power_w_max": max(float(r[3]) for r in rows if r[3].replace(".", "").isdigit())}
 
 
+def max_over_ranks(x: float, dist, device) -> float:
+    """The largest of every rank's x (the job's time is its slowest replica's); x itself when not
+    distributed.  `device` holds the reduction tensor: "cuda" under NCCL, "cpu" under gloo."""
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_gteps(ranks: int, edges: int, steps: int, total_ms: float) -> float:
+    """Whole-job TEPS in G: every replica counts `edges` undirected edges per step."""
+    return ranks * edges * steps / (total_ms * 1e-3) / 1e9
+
+
 def _dist():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -246,10 +262,7 @@ def run_ours(args, ws, rank, local):
     clocks = clk.summary()
     step_ms = [a.elapsed_time(b) for a, b in ev]
     total_ms = sum(step_ms)
-    if dist:
-        t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(total_ms, dist, "cuda")
     ok = all(r.triangles == expect_count for r in res)
     count_s = statistics.median(r.count_seconds for r in res)
     kernel_s = statistics.median(r.kernel_seconds for r in res)
@@ -305,7 +318,7 @@ def run_ours(args, ws, rank, local):
     achieved = algo_bytes / count_s / 1e9
     line = {
         "metric": METRIC,
-        "value": ws * m * args.steps / (total_ms * 1e-3) / 1e9,
+        "value": job_gteps(ws, m, args.steps, total_ms),
         "unit": "GTEPS",
         "n_gpus": ws,
         "steps": args.steps,
@@ -431,7 +444,7 @@ def run_batch(args, ws, rank, local):
     algo_bytes = 24 * m + 8 * (n + 1) + 4 * r.wedges
     line = {
         "metric": METRIC,
-        "value": ws * m * steps / (total_ms * 1e-3) / 1e9,
+        "value": job_gteps(ws, m, steps, total_ms),
         "unit": "GTEPS",
         "n_gpus": ws,
         "steps": steps,
