@@ -70,7 +70,8 @@ typedef struct trust_tc_opts {
   int ptr_kind;          /* TRUST_TC_HOST or TRUST_TC_DEVICE                                     */
   int schedule;          /* TRUST_TC_SCHED_*                                                     */
   int validate;          /* TRUST_TC_VALIDATE_* (device input); default FULL                     */
-  int warp_max_degree;   /* out-degree above which a vertex gets a whole CTA; 0 = default       */
+  int warp_max_degree;   /* out-degree above which a vertex gets a whole CTA; 0 = default (512;
+                            100 under TRUST_TC_SCHED_PLAIN)                                   */
   int block_max_degree;  /* out-degree above which a vertex gets a cluster table; 0 = default   */
   int record_cycles;     /* 1: write per-vertex clock64 cycles into result->vertex_cycles       */
   void *stream;          /* cudaStream_t; NULL = legacy default stream                          */

@@ -118,8 +118,11 @@ struct LaunchCfg {
 static int resolve_cfg(trust_tc_ctx *c, const trust_tc_opts &o, bool same, LaunchCfg *cfg) {
   cfg->threads = o.threads_per_block > 0 ? o.threads_per_block : 256;
   if (cfg->threads % 32 || cfg->threads < 64 || cfg->threads > 1024) return TRUST_TC_E_ARG;
-  // the plain schedule is the reference's split: a warp per vertex up to out-degree 100 (USE_CTA)
-  cfg->warp_max = o.warp_max_degree > 0 ? o.warp_max_degree : (o.schedule == TRUST_TC_SCHED_PLAIN ? 100 : 128);
+  // the plain schedule is the reference's split: a warp per vertex up to out-degree 100 (USE_CTA);
+  // the tuned and learned classes give a warp rows of up to 512 entries (measured on R-MAT 22 /
+  // 24 / 26 with the learned schedule: 13 % / 5 % / 2 % faster than 128, since CTA-class rows pay
+  // a CTA barrier per vertex; 1024 loses occupancy to 64 KiB of warp tables)
+  cfg->warp_max = o.warp_max_degree > 0 ? o.warp_max_degree : (o.schedule == TRUST_TC_SCHED_PLAIN ? 100 : 512);
   if (cfg->warp_max < 32 || cfg->warp_max > 4096) return TRUST_TC_E_ARG;
   int want_cta = o.block_max_degree > 0 ? o.block_max_degree : 4096;
   if (want_cta < cfg->warp_max) return TRUST_TC_E_ARG;
@@ -141,8 +144,9 @@ static int resolve_cfg(trust_tc_ctx *c, const trust_tc_opts &o, bool same, Launc
 }
 
 // The learned schedule promotes a warp-class row to a CTA when its predicted cost exceeds
-// 2^TC_PROMOTE_LOG2 cycles (about half a millisecond at the GB300 clock).
-constexpr float TC_PROMOTE_LOG2 = 20.f;
+// 2^TC_PROMOTE_LOG2 cycles (about 2 ms at the GB300 clock: only rows that would hold one warp
+// far longer than the rest of the queue).
+constexpr float TC_PROMOTE_LOG2 = 22.f;
 
 // Below this many arcs the learned schedule's scheduling pass (about 0.1-0.3 ms on GB300) cannot
 // be repaid: the whole count takes about 2 ms or less, and the measured split gain on R-MAT
@@ -311,7 +315,9 @@ int count_device(trust_tc_ctx *c, const DevGraph3 &g, const trust_tc_opts &o, bo
   }
   // shared memory sized to what this graph needs: warp tables, plus a CTA table only as large as
   // the largest CTA-class row present; the rest of the SM's unified memory stays L1
-  size_t smem = (size_t)4 * cfg.warp_slots * (cfg.threads / 32);
+  // warp tables sized to the largest row a warp can get here (>= 128 slots: 4G for G32 groups)
+  const int warp_slots = 1 << std::max(ceil_log2_size(2 * std::min<int64_t>(table_max, cfg.warp_max)), 7);
+  size_t smem = (size_t)4 * warp_slots * (cfg.threads / 32);
   if (h.class_count[TC_CLASS_CTA] > 0) {
     const int64_t dcta = std::min<int64_t>(h.max_out_degree, cfg.cta_max);
     smem = std::max(smem, (size_t)4 << std::max(ceil_log2_size(2 * dcta), 6));
@@ -341,7 +347,7 @@ int count_device(trust_tc_ctx *c, const DevGraph3 &g, const trust_tc_opts &o, bo
   a.off = off;
   a.ctl = ctl;
   a.huge_tables = c->d_huge;
-  a.warp_slots = cfg.warp_slots;
+  a.warp_slots = warp_slots;
   a.chunk = cfg.chunk;
   a.split = split;
   a.rowmap = g.rowmap;

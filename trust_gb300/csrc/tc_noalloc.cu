@@ -79,7 +79,8 @@ extern "C" int trust_tc_count_csr_noalloc(const int64_t *d_begin, const int32_t 
   TC_CUDA_TRY(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, device));
   TC_CUDA_TRY(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device));
   const int threads = o.threads_per_block > 0 ? o.threads_per_block : 256;
-  const int warp_max = o.warp_max_degree > 0 ? o.warp_max_degree : 128;
+  const int warp_max =
+      o.warp_max_degree > 0 ? o.warp_max_degree : (o.schedule == TRUST_TC_SCHED_PLAIN ? 100 : 512);
   const int want_cta = o.block_max_degree > 0 ? o.block_max_degree : 4096;
   if (threads % 32 || threads < 64 || threads > 1024 || warp_max < 32 || warp_max > 4096 || want_cta < warp_max)
     return TRUST_TC_E_ARG;
@@ -103,7 +104,7 @@ extern "C" int trust_tc_count_csr_noalloc(const int64_t *d_begin, const int32_t 
   rc = tc::launch_check(d_begin, d_adj, n, m, n, o.validate >= TRUST_TC_VALIDATE_FULL, ctl, num_sms, st);
   if (rc) return rc;
   tc::ListOffsets off{};
-  rc = tc::launch_classify(0, d_begin, d_begin, n, 2, warp_max, cta_max, ctl, lists, off, num_sms, st);
+  rc = tc::launch_classify(0, d_begin, d_begin, n, 2, warp_max, cta_max, ctl, lists, off, num_sms, st, o.schedule);
   if (rc) return rc;
   TcControl h;
   TC_CUDA_TRY(cudaMemcpyAsync(&h, ctl, sizeof h, cudaMemcpyDeviceToHost, st));
@@ -118,7 +119,7 @@ extern "C" int trust_tc_count_csr_noalloc(const int64_t *d_begin, const int32_t 
     off.off[k] = (int)total;
     total += h.class_count[k];
   }
-  rc = tc::launch_classify(1, d_begin, d_begin, n, 2, warp_max, cta_max, ctl, lists, off, num_sms, st);
+  rc = tc::launch_classify(1, d_begin, d_begin, n, 2, warp_max, cta_max, ctl, lists, off, num_sms, st, o.schedule);
   if (rc) return rc;
   tc::CountArgs a{};
   a.begA = a.begB = a.begC = d_begin;
