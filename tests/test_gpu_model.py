@@ -94,25 +94,34 @@ def test_learned_schedule_exact_with_any_model(seed):
 
 
 def test_learned_schedule_gain_on_skewed_rmat():
-    """What the trained network buys over the plain degree-threshold schedule on a skewed graph
-    (R-MAT scale 20, edge factor 16): the same count, the reverse-direction pass chosen from the
-    model's predicted saving, and a shorter call (measured 7.3 ms vs 10.1 ms on GB300; asserted
-    with a wide margin)."""
+    """What the trained network buys on a skewed graph (R-MAT scale 20, edge factor 16), against
+    (a) the plain degree-threshold schedule and (b) the same learned schedule with a network that
+    predicts nothing (all weights zero: every row at 1 cycle, so no predicted saving and no
+    direction split).  Same count every time; the trained network's predicted saving turns the
+    reverse-direction pass on and the call gets shorter (measured 6.9 ms vs 10.1 ms plain and
+    8.2 ms without the network, on GB300; asserted with wide margins)."""
     import statistics
     pairs = T.gen_rmat(20, 16, seed=3)
     beg, adj = T.build_csr(pairs, 1 << 20)
     del pairs
+    blind = np.zeros(mlp.FLOATS, dtype=np.float32)
+    blind[mlp.OFF_ISCALE:mlp.OFF_ISCALE + 8] = 1.0
+    blind[mlp.OFF_YSCALE] = 1.0
     times = {}
     counts = {}
     with T.Context() as ctx:
-        for name, sched in (("plain", T.SCHED_PLAIN), ("learned", T.SCHED_LEARNED)):
+        for name, sched, model in (("plain", T.SCHED_PLAIN, None), ("learned", T.SCHED_LEARNED, None),
+                                   ("no_network", T.SCHED_LEARNED, blind)):
             ts = []
             for _ in range(5):
-                r = T.count_csr(beg, adj, ctx=ctx, schedule=sched)
+                r = T.count_csr(beg, adj, ctx=ctx, schedule=sched, model=model)
                 ts.append(r.call_seconds)
             times[name] = statistics.median(ts)
             counts[name] = r.triangles
             if name == "learned":
                 assert r.direction_split and r.split_saving_ms > 1.0
-    assert counts["learned"] == counts["plain"]
+            if name == "no_network":
+                assert not r.direction_split and r.split_saving_ms < 0.01
+    assert counts["learned"] == counts["plain"] == counts["no_network"]
     assert times["learned"] < 0.85 * times["plain"], times
+    assert times["learned"] < 0.95 * times["no_network"], times
