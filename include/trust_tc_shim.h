@@ -3,11 +3,11 @@
  *
  * Declares the same `struct arguments` and `Triangle_count` as Without-graph-partition/TC.cuh:2-10
  * (C++ linkage), plus the partitioned overload of With-graph-partition/TC.cuh:10, so a non-MPI
- * driver written like Without-graph-partition/mpi_main.cpp:84-128 links against libtrust_tc.so
- * unchanged.  Error behaviour matches the reference's HRR macro (Without-graph-partition/
+ * main program written like Without-graph-partition/mpi_main.cpp:84-128 links against
+ * libtrust_tc.so unchanged.  Error behaviour matches the reference's HRR macro (Without-graph-partition/
  * herror.h:1-8): the message is printed and the process exits with EXIT_FAILURE.  Logical ranks:
- * this build counts on one GPU, so rank 0 returns the whole count and ranks > 0 return 0 (the
- * driver's SUM over ranks, mpi_main.cpp:119, is unchanged).
+ * the library counts on one GPU, so rank 0 returns the whole count and ranks > 0 return 0 (the
+ * main program's SUM over ranks, mpi_main.cpp:119, is unchanged).
  */
 #ifndef TRUST_TC_SHIM_H
 #define TRUST_TC_SHIM_H

@@ -5,7 +5,7 @@ Outputs (all git-ignored):
                                include/trust_tc_shim.h, kernels compiled for sm_103a only
   trust_gb300/trust_tc         the CLI with the reference's argv and output line
   oracle/_build/liboracle.so   CPU oracle (tests, smoke and the bench CPU legs only)
-  oracle/_build/liboracle_cuda.so  oracle + the driver that runs the reference kernel cubin
+  oracle/_build/liboracle_cuda.so  oracle + the harness that runs the reference kernel cubin
   oracle/_ref/*                the reference's own code, only where its sources are present
 
 Compiles in parallel and skips outputs newer than their sources.

@@ -1,4 +1,4 @@
-// tc_cli.cpp — command-line driver with the reference's argv and output line.
+// tc_cli.cpp — command-line program with the reference's argv and output line.
 //
 //   trust_tc <folder> <nGPUs> <threads> <blocks> <chunk>          (Without-graph-partition/mpi_main.cpp:84-128)
 //   trust_tc <folder> <nGPUs> <threads> <blocks> <chunk> <n>      (With-graph-partition/mpi_main.cpp:75-127)
