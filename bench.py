@@ -43,7 +43,7 @@ WORKLOADS = {
                    desc="R-MAT scale 22 edge factor 16 (0.57,0.19,0.19,0.05) seed=3"),
     "rmat24_a070": dict(kind="rmat", scale=24, ef=16, a=0.70, b=0.125, c=0.125, seed=3,
                         desc="R-MAT scale 24 edge factor 16 (0.70,0.125,0.125,0.05) seed=3 (cost model held out)"),
-    "rmat26_ef32": dict(kind="rmat", scale=26, ef=32, a=0.57, b=0.19, c=0.19, seed=3,
+    "rmat26_ef32": dict(kind="rmat", scale=26, ef=32, a=0.57, b=0.19, c=0.19, seed=3, tiles=2,
                         desc="R-MAT scale 26 edge factor 32 (0.57,0.19,0.19,0.05) seed=3"),
     "batch4096": dict(kind="batch", graphs=4096, nmin=50, nmax=50_000, seed=5,
                       desc="4096 graphs, vertices log-uniform 50..50,000, alternately Erdos-Renyi (avg degree "
@@ -292,6 +292,21 @@ def run_ours(args, ws, rank, local):
         if name == "autotuned":
             sched[name]["launch"] = tuned_cfg
 
+    # the n x n tile loop on the same graph (once per mode, outside the timed region): tiles in HBM
+    # under the learned and the plain schedule, and streamed through a 3.5-tile device budget
+    tiles = args.tiles if args.tiles is not None else w.get("tiles", 0)
+    tile_loop = None
+    if tiles > 1:
+        tile_bytes = (8 * (n + 1) + 4 * m) // (tiles * tiles)
+        tile_loop = {"parts": tiles, "jobs": tiles ** 3}
+        for name, sch, budget in (("learned", T.SCHED_LEARNED, 0), ("plain", T.SCHED_PLAIN, 0),
+                                  ("learned_streamed", T.SCHED_LEARNED, 3 * tile_bytes + (tile_bytes >> 1))):
+            rt = T.count_tiles(beg, adj, tiles, budget_bytes=budget, schedule=sch)
+            ok = ok and rt.triangles == expect_count
+            tile_loop[name] = {"s": rt.call_seconds, "gteps": m / rt.call_seconds / 1e9,
+                               "split_jobs": rt.direction_split, "wedges": rt.wedges, "budget_bytes": budget}
+        tile_loop["learned_vs_plain"] = tile_loop["plain"]["s"] / tile_loop["learned"]["s"]
+
     # end to end through the C ABI: pinned host buffers, H2D + count + result read inside the region
     hb = beg.cpu().pin_memory()
     ha = adj.cpu().pin_memory()
@@ -351,6 +366,8 @@ def run_ours(args, ws, rank, local):
         "preprocess": {"gpu_generate_ms": prep["generate_ms"], "gpu_build_csr_ms": prep["preprocess_ms"]},
         "clocks": clocks,
     }
+    if tile_loop:
+        line["tile_loop"] = tile_loop
     if ws == 1 and not args.no_cpu_baseline:
         cb, cpu_count = cpu_baseline(beg.cpu().numpy(), adj.cpu().numpy())
         line["cpu_baseline"] = cb
@@ -543,6 +560,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default=DEFAULT_WORKLOAD)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--tiles", type=int, default=None,
+                    help="also run the parts x parts tile loop (default: 2 for rmat26_ef32, else off)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -78,7 +78,9 @@ typedef struct trust_tc_opts {
   const float *model;    /* learned schedule: packed MLP weights (trust_tc_model_size floats)   */
   int direction_split;   /* charge arcs with d(u) > d(v) to u's side (hash N+(u), stream N+(v)):
                             -1 = the learned schedule decides, 0 = never, 1 = always; applied only
-                            when every row is strictly increasing (duplicate-free)             */
+                            when every row is strictly increasing (duplicate-free).  In the tile
+                            loop a job (i,j,k) charges arc (v,u) to u's side when its probe row
+                            in tile (k,j) is longer than v's table row in tile (i,j)          */
   int hub_cluster;       /* rows above the CTA table (out-degree > 4096): 0 = in shared memory,
                             one CTA while the table fits in 64 KiB, else a thread-block cluster
                             with the table split over its CTAs (distributed shared memory);
@@ -96,7 +98,8 @@ typedef struct trust_tc_result {
   int64_t wedges;           /* sum over arcs (v,u) with d(v)>=2 of d(u): the probe count     */
   int64_t class_sizes[8];   /* vertices per schedule class (skip, g4, g8, g16, g32, warp, cta, cluster) */
   uint64_t *vertex_cycles;  /* caller-provided device array of n entries, or NULL            */
-  int32_t direction_split;  /* 1 when the second (reverse-direction) pass ran                 */
+  int32_t direction_split;  /* 1 when the second (reverse-direction) pass ran (tile loop: the
+                               number of jobs that ran it)                                  */
   float split_saving_ms;    /* learned schedule: predicted saving of that pass, ms (else 0)  */
 } trust_tc_result;
 

@@ -53,14 +53,14 @@ class CountResult:
     max_out_degree: int
     wedges: int = 0
     class_sizes: dict = field(default_factory=dict)
-    direction_split: bool = False
+    direction_split: int = 0  # 1 when the reverse-direction pass ran (tile loop: jobs that ran it)
     split_saving_ms: float = 0.0
 
 
 def _result(r: _lib.Result) -> CountResult:
     return CountResult(int(r.triangles), r.kernel_seconds, r.count_seconds, r.call_seconds, int(r.vertices),
                        int(r.edges), int(r.max_out_degree), int(r.wedges),
-                       {k: int(v) for k, v in zip(CLASS_NAMES, r.class_sizes)}, bool(r.direction_split),
+                       {k: int(v) for k, v in zip(CLASS_NAMES, r.class_sizes)}, int(r.direction_split),
                        float(r.split_saving_ms))
 
 
@@ -154,8 +154,10 @@ def count_folder(folder: str, threads=0, blocks=0, chunk=0) -> CountResult:
     return _result(r)
 
 
-def count_partitioned(folder: str, parts: int, threads=0, blocks=0, chunk=0) -> CountResult:
-    o = _opts(threads, blocks, chunk)
+def count_partitioned(folder: str, parts: int, threads=0, blocks=0, chunk=0, schedule=SCHED_LEARNED,
+                      direction_split: int = -1) -> CountResult:
+    o = _opts(threads, blocks, chunk, schedule=schedule)
+    o.direction_split = direction_split
     r = _lib.Result()
     check(load().trust_tc_count_partitioned(folder.encode(), parts, C.byref(o), C.byref(r)),
           "trust_tc_count_partitioned")
@@ -175,10 +177,13 @@ def autotune(beg, adj, ctx: Context, repeats: int = 3, schedule=SCHED_LEARNED) -
 
 
 def count_tiles(beg, adj, parts: int, budget_bytes: int = 0, threads=0, blocks=0, chunk=0,
-                schedule=SCHED_LEARNED) -> CountResult:
+                schedule=SCHED_LEARNED, direction_split: int = -1) -> CountResult:
     """The n x n tile loop over a device CSR (torch CUDA tensors): GPU partition into pinned host
-    tiles, then the (i,j,k) jobs with tiles streamed into a device cache of `budget_bytes`."""
+    tiles, then the (i,j,k) jobs with tiles streamed into a device cache of `budget_bytes`.
+    `direction_split`: -1 the schedule decides per job, 0 never, 1 every job whose tiles allow it
+    (`CountResult.direction_split` = the jobs that ran it)."""
     o = _opts(threads, blocks, chunk, DEVICE, schedule=schedule)
+    o.direction_split = direction_split
     r = _lib.Result()
     check(load().trust_tc_count_tiles_device(C.c_void_p(beg.data_ptr()), C.c_void_p(adj.data_ptr()), beg.numel() - 1,
                                              adj.numel(), parts, budget_bytes, C.byref(o), C.byref(r)),

@@ -273,6 +273,20 @@ int count_device(trust_tc_ctx *c, const DevGraph3 &g, const trust_tc_opts &o, bo
       split = sorted && split_pays(plan.w_all, plan.w_min, g.mA, g.rows);
     }
   }
+  // a tile job (three CSRs, duplicate-free tables and probe rows): the same split, decided by the
+  // probe totals of its plan
+  const bool consider3 = !same && g.split_ok && !g.rowmap && g.rows > 0 && g.min_deg == 1 &&
+                         (o.direction_split == 1 ||
+                          (o.direction_split < 0 && o.schedule == TRUST_TC_SCHED_LEARNED &&
+                           h.max_out_degree >= 64 && g.mB >= TC_LEARNED_MIN_ARCS));
+  if (consider3) {
+    rc = tile_split_plan(c, g, st);
+    if (rc) return rc;
+    TC_CUDA_TRY(cudaStreamSynchronize(st));
+    SchedPlan plan{};
+    split_plan_read(c, &plan);
+    split = o.direction_split == 1 || split_pays(plan.w_all, plan.w_min, g.mB, g.rows);
+  }
   int64_t total = 0;
   for (int k = TC_CLASS_SKIP + 1; k < TC_NUM_CLASSES; ++k) {
     off.off[k] = (int)total;
@@ -390,21 +404,29 @@ int count_device(trust_tc_ctx *c, const DevGraph3 &g, const trust_tc_opts &o, bo
   r->split_saving_ms = saving_ms;
   if (split) {
     // second pass: arcs (v,u) with d(u) > d(v), hashed on u's row, streaming the sources' rows
+    // (a tile job: tables from C's rows, probe rows from A's)
     SplitRows sr{};
     TC_CUDA_TRY(cudaEventRecord(c->ev_split[0], st));
-    rc = split_build(c, g.begA, g.adjA, g.rows, g.mA, st, &sr);
+    rc = same ? split_build(c, g.begA, g.adjA, g.rows, g.mA, st, &sr)
+              : split_build(c, g.begC, g.adjC, g.rowsC, g.mB, st, &sr);
     if (rc) return rc;
     TC_CUDA_TRY(cudaEventRecord(c->ev_split[1], st));
     DevGraph3 gb = g;
+    if (!same) {
+      gb.begA = g.begC; gb.adjA = g.adjC; gb.mA = g.mC; gb.boundA = g.boundC;
+      gb.begC = g.begA; gb.adjC = g.adjA; gb.mC = g.mA; gb.boundC = g.boundA;
+      gb.rowsC = g.rows;
+    }
     gb.begB = sr.beg;
     gb.adjB = sr.adj;
     gb.mB = sr.m;
     gb.boundB = g.rows;
     gb.rowmap = sr.rowmap;
-    gb.rowsA = g.rows;
+    gb.rowsA = same ? g.rows : g.rowsC;
     gb.rows = sr.rows;
     gb.min_deg = 1;
-    gb.max_deg_A = h.max_out_degree;  // tables are rows of the graph itself, not in-list chunks
+    gb.split_ok = 0;
+    gb.max_deg_A = h.max_out_degree;  // tables are whole rows (of the graph, or of C), not in-list chunks
     trust_tc_opts ob = o;
     ob.schedule = TRUST_TC_SCHED_TUNED;
     ob.record_cycles = 0;

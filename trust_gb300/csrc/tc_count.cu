@@ -555,7 +555,7 @@ __device__ void cta_vertex(const CountArgs &p, int v, int *tab, BlockShared &bs,
     const int i = (bt << 5) + lane;
     int s = 0, dd = 0;
     if (i < dB) row_of(p.begC, tc_ld_nc(p.adjB + bB + i), s, dd);
-    if (SAME && p.split && dd > dB) dd = 0;
+    if (p.split && dd > dA) dd = 0;
     if (longs) {
       const bool lg = dd >= TC_CTA_LONG;
       const unsigned lm = __ballot_sync(TC_FULL_MASK, lg);
@@ -608,7 +608,7 @@ __device__ __forceinline__ void warp_vertex(const CountArgs &p, int v, int *warp
     const int i = a0 + lane;
     int s = 0, dd = 0;
     if (i < dB) row_of(p.begC, tc_ld_nc(p.adjB + bB + i), s, dd);
-    if (SAME && p.split && dd > dB) dd = 0;
+    if (p.split && dd > dA) dd = 0;
     probe_arcs<32, LongRow<32>::value>(p.adjC, s, dd, lane, set, hits, wedges);
   }
   __syncwarp();
@@ -678,7 +678,7 @@ __device__ void drain_group_class(const CountArgs &p, int c, int *warp_tab, unsi
   auto ld_target = [&](GroupStage &x) {
     x.s = 0; x.dd = 0;
     if (x.uB >= 0) row_of(p.begC, x.uB, x.s, x.dd);
-    if (SAME && p.split && x.dd > x.d) x.dd = 0;  // counted from u's side in the second pass
+    if (p.split && x.dd > x.d) x.dd = 0;  // counted from u's side in the second pass
   };
   for (;;) {
     int t0 = 0;
@@ -980,7 +980,7 @@ __global__ void __launch_bounds__(512, 1) hub_kernel(CountArgs p, int log2C, int
       const int i = (bt << 5) + lane;
       int s = 0, dd = 0;
       if (i < dB) row_of(p.begC, tc_ld_nc(p.adjB + bB + i), s, dd);
-      if (SAME && p.split && dd > dB) dd = 0;
+      if (p.split && dd > dA) dd = 0;
       probe_arcs<32, LongRow<32>::value>(p.adjC, s, dd, lane, set, hits, wedges);
     }
     cl.sync();  // every probe of this hub is done before any share is cleared again

@@ -25,7 +25,8 @@ struct CountArgs {
   int warp_slots;     // shared-memory ints per warp in the warp phase
   int chunk;          // items per queue claim (per group) in the warp phase
   unsigned long long *cycles;  // optional: per-row clock64 cycles (rows * 1 entries) or null
-  int split;          // 1: skip arcs (v,u) with d(u) > d(v); a second pass counts them from u's side
+  int split;          // 1: skip arcs (v,u) whose probe row C[u] is longer than the table row A[v];
+                      // a second pass counts them from u's side
   const int *rowmap;  // optional: table row (A) of each work row (B); null = the same index
   int2 *long_rows;    // optional: per-CTA lists of deferred long neighbour rows (row start, length)
   int long_cap;       // entries per CTA in long_rows (>= the largest CTA-class out-degree)

@@ -75,6 +75,8 @@ struct DevGraph3 {
   int64_t boundA, boundB, boundC;  // exclusive id bound per CSR (B's ids index rows of C)
   int min_deg;                // rows with fewer entries in A or B are skipped
   int64_t max_deg_A;          // largest row of A when known (0: the validation pass's maximum)
+  int split_ok;               // three distinct CSRs whose A and C rows are duplicate-free: the
+                              // direction split may count an arc from C's side
 };
 
 int ctx_init(trust_tc_ctx *c, int device);
@@ -120,5 +122,11 @@ struct SplitRows {
 };
 int split_build(trust_tc_ctx *c, const int64_t *beg, const int32_t *adj, int64_t n, int64_t m, cudaStream_t st,
                 SplitRows *out);
+// The split plan of a job over three CSRs (tile jobs): probe totals and the arcs of B to move,
+// read back like split_plan's.
+int tile_split_plan(trust_tc_ctx *c, const DevGraph3 &g, cudaStream_t st);
+// Whether every row of a CSR is strictly increasing (so duplicate-free); synchronous.
+int rows_increasing(trust_tc_ctx *c, const int64_t *beg, const int32_t *adj, int64_t rows, cudaStream_t st,
+                    bool *out);
 
 }  // namespace tc

@@ -457,6 +457,103 @@ void split_plan_read(const trust_tc_ctx *c, SchedPlan *plan) {
   plan->moved_arcs = (int64_t)c->h_plans[PLAN_NPAIRS];
 }
 
+// ---- tile jobs: three CSRs ---------------------------------------------------------------------
+// A tile job (i,j,k) hashes table rows A[v] (tile (i,j)), walks the arcs (v,u) of B[v] (tile
+// (i,k)) and streams probe rows C[u] (tile (k,j)); an arc costs |C[u]| probes.  Counted from u's
+// side (hash C[u], stream A[v]) it costs |A[v]|, and |A[v] ∩ C[u]| is the same number when both
+// rows are duplicate-free.  The plan moves every arc with |C[u]| > |A[v]| of a row with A[v]
+// nonempty (rows with A[v] empty contribute nothing from either side).  One warp per row of B:
+// tile rows are short, and the pass is a small fraction of the job's counting.
+__global__ void tile_sched_kernel(const int64_t *__restrict__ begA, const int64_t *__restrict__ begB,
+                                  const int32_t *__restrict__ adjB, const int64_t *__restrict__ begC, int64_t rows,
+                                  unsigned *__restrict__ cnt, unsigned long long *__restrict__ wsum,
+                                  unsigned long long *plans, int2 *__restrict__ pairs, unsigned *__restrict__ ranks) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  unsigned long long w_all = 0, w_min = 0;
+  for (int64_t v = warp; v < rows; v += nwarps) {
+    const int dA = (int)(tc_ld_nc(begA + v + 1) - tc_ld_nc(begA + v));
+    if (dA < 1) continue;
+    const long long b0 = tc_ld_nc(begB + v);
+    const int dB = (int)(tc_ld_nc(begB + v + 1) - b0);
+    for (int i0 = 0; i0 < dB; i0 += 32) {
+      const int i = i0 + lane;
+      int u = 0, du = 0;
+      if (i < dB) {
+        u = tc_ld_nc(adjB + b0 + i);
+        du = (int)(tc_ld_nc(begC + u + 1) - tc_ld_nc(begC + u));
+        w_all += (unsigned)du;
+        w_min += (unsigned)min(du, dA);
+      }
+      move_arc(i < dB && du > dA, u, (int)v, dA, cnt, wsum, pairs, ranks, plans + PLAN_NPAIRS);
+    }
+  }
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) {
+    w_all += __shfl_down_sync(TC_FULL_MASK, w_all, o);
+    w_min += __shfl_down_sync(TC_FULL_MASK, w_min, o);
+  }
+  if (lane == 0) {
+    if (w_all) atomicAdd(plans + PLAN_W_ALL, w_all);
+    if (w_min) atomicAdd(plans + PLAN_W_MIN, w_min);
+  }
+}
+
+int tile_split_plan(trust_tc_ctx *c, const DevGraph3 &g, cudaStream_t st) {
+  const size_t nt = (size_t)std::max<int64_t>(g.rowsC + 1, 1);  // targets u: rows of C
+  int rc = ensure((void **)&c->d_split_cnt, &c->split_cnt_cap, sizeof(unsigned) * nt);
+  if (rc) return rc;
+  if ((rc = ensure((void **)&c->d_split_plans, &c->split_plans_cap, TC_PLAN_WORDS * sizeof(unsigned long long))))
+    return rc;
+  if ((rc = ensure((void **)&c->d_split_wsum, &c->split_wsum_cap, sizeof(unsigned long long) * nt))) return rc;
+  const size_t mb = (size_t)std::max<int64_t>(g.mB, 1);
+  if ((rc = ensure((void **)&c->d_split_pairs, &c->split_pairs_cap, sizeof(int2) * mb))) return rc;
+  if ((rc = ensure((void **)&c->d_split_ranks, &c->split_ranks_cap, sizeof(unsigned) * mb))) return rc;
+  TC_CUDA_TRY(cudaMemsetAsync(c->d_split_cnt, 0, sizeof(unsigned) * nt, st));
+  TC_CUDA_TRY(cudaMemsetAsync(c->d_split_wsum, 0, sizeof(unsigned long long) * nt, st));
+  TC_CUDA_TRY(cudaMemsetAsync(c->d_split_plans, 0, TC_PLAN_WORDS * sizeof(unsigned long long), st));
+  const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((g.rows + 7) / 8, (int64_t)c->num_sms * 8));
+  tile_sched_kernel<<<blocks, 256, 0, st>>>(g.begA, g.begB, g.adjB, g.begC, g.rows, c->d_split_cnt, c->d_split_wsum,
+                                            c->d_split_plans, c->d_split_pairs, c->d_split_ranks);
+  TC_NOTE_LAUNCH();
+  TC_CUDA_TRY(cudaGetLastError());
+  TC_CUDA_TRY(cudaMemcpyAsync(c->h_plans, c->d_split_plans, TC_PLAN_WORDS * sizeof(unsigned long long),
+                              cudaMemcpyDeviceToHost, st));
+  return TRUST_TC_OK;
+}
+
+// One warp per row: any entry not below its successor marks the CSR (flag word 1).
+__global__ void rows_increasing_kernel(const int64_t *__restrict__ beg, const int32_t *__restrict__ adj,
+                                       int64_t rows, unsigned long long *flag) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  int bad = 0;
+  for (int64_t v = warp; v < rows; v += nwarps) {
+    const long long b = tc_ld_nc(beg + v);
+    const int d = (int)(tc_ld_nc(beg + v + 1) - b);
+    for (int k = lane; k + 1 < d; k += 32) bad |= tc_ld_nc(adj + b + k) >= tc_ld_nc(adj + b + k + 1);
+  }
+  bad = __reduce_or_sync(TC_FULL_MASK, bad);
+  if (lane == 0 && bad) atomicOr(flag, 1ull);
+}
+
+int rows_increasing(trust_tc_ctx *c, const int64_t *beg, const int32_t *adj, int64_t rows, cudaStream_t st,
+                    bool *out) {
+  int rc = ensure((void **)&c->d_split_plans, &c->split_plans_cap, TC_PLAN_WORDS * sizeof(unsigned long long));
+  if (rc) return rc;
+  TC_CUDA_TRY(cudaMemsetAsync(c->d_split_plans, 0, sizeof(unsigned long long), st));
+  const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((rows + 7) / 8, (int64_t)c->num_sms * 8));
+  rows_increasing_kernel<<<blocks, 256, 0, st>>>(beg, adj, rows, c->d_split_plans);
+  TC_NOTE_LAUNCH();
+  TC_CUDA_TRY(cudaGetLastError());
+  TC_CUDA_TRY(cudaMemcpyAsync(c->h_plans, c->d_split_plans, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+  TC_CUDA_TRY(cudaStreamSynchronize(st));
+  *out = c->h_plans[0] == 0;
+  return TRUST_TC_OK;
+}
+
 // Build the second pass's work rows (after split_plan, whose long-row list it reuses): the
 // in-list of every target, cut into chunks so one heavily targeted row spreads over many CTAs.
 // Outputs live in the context.

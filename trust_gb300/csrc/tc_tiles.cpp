@@ -118,6 +118,9 @@ int tile_loop(const std::vector<HostTile> &ht, int p, const trust_tc_opts &o, si
     return false;
   };
   uint64_t copied = 0;
+  // per tile: rows strictly increasing (so duplicate-free), checked on its first copy; the
+  // direction split of a job needs it of the job's table and probe tiles
+  std::vector<signed char> increasing((size_t)p * p, -1);
   auto fetch = [&](int id, int k0, int k1, int k2) -> int {
     DevTile &d = dt[id];
     if (d.resident) {
@@ -144,6 +147,12 @@ int tile_loop(const std::vector<HostTile> &ht, int p, const trust_tc_opts &o, si
     d.resident = true;
     used += bytes;
     lru.push_front(id);
+    if (increasing[id] < 0) {
+      bool inc = false;
+      const int rc2 = rows_increasing(&ctx, d.beg, d.adj, h.rows, (cudaStream_t)o.stream, &inc);
+      if (rc2) return rc2;
+      increasing[id] = inc ? 1 : 0;
+    }
     return TRUST_TC_OK;
   };
   uint64_t *cycles = r->vertex_cycles;
@@ -172,7 +181,9 @@ int tile_loop(const std::vector<HostTile> &ht, int p, const trust_tc_opts &o, si
         g.rowsC = ht[C].rows;
         g.mA = ht[A].m; g.mB = ht[Bt].m; g.mC = ht[C].m;
         g.boundA = NOBOUND; g.boundB = ht[C].rows; g.boundC = NOBOUND;
-        g.min_deg = 1;
+        // a diagonal job (i,i,i) is one CSR: rows with one entry close no triangle there
+        g.min_deg = (A == Bt && Bt == C) ? 2 : 1;
+        g.split_ok = increasing[A] == 1 && increasing[C] == 1;
         trust_tc_result jr;
         memset(&jr, 0, sizeof jr);
         rc = count_device(&ctx, g, o, true, &jr);
@@ -181,6 +192,8 @@ int tile_loop(const std::vector<HostTile> &ht, int p, const trust_tc_opts &o, si
         tk += jr.kernel_seconds;
         tcount += jr.count_seconds;
         r->max_out_degree = std::max(r->max_out_degree, jr.max_out_degree);
+        r->direction_split += jr.direction_split;  // jobs counted with the split
+        r->split_saving_ms += jr.split_saving_ms;
         for (int c = 0; c < TC_NUM_CLASSES; ++c) r->class_sizes[c] += jr.class_sizes[c];
       }
   cudaEventRecord(e1, (cudaStream_t)o.stream);
