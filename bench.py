@@ -307,12 +307,16 @@ def run_ours(args, ws, rank, local):
                                "split_jobs": rt.direction_split, "wedges": rt.wedges, "budget_bytes": budget}
         tile_loop["learned_vs_plain"] = tile_loop["plain"]["s"] / tile_loop["learned"]["s"]
 
-    # end to end through the C ABI: pinned host buffers, H2D + count + result read inside the region
+    # end to end through the C ABI: pinned host buffers, every step's H2D copy, count and result
+    # read inside the timed region.  Serial: copy then count, one call per step.  Pipelined (the
+    # reported e2e): step i+1's copy is staged on the context's copy stream (trust_tc_stage_csr)
+    # before step i is counted, as a caller streaming graphs does; L2 flushed before every count.
     hb = beg.cpu().pin_memory()
     ha = adj.cpu().pin_memory()
     hb_np, ha_np = hb.numpy(), ha.numpy()
     e2e_ev = []
-    for i in range(max(3, args.steps // 4) + 2):
+    k_e2e = max(3, args.steps // 4)
+    for i in range(k_e2e + 2):
         flush.fill_(i)
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record(stream)
@@ -322,7 +326,23 @@ def run_ours(args, ws, rank, local):
         e2e_ev.append((a, b))
     torch.cuda.synchronize()
     e2e_ms = [a.elapsed_time(b) for a, b in e2e_ev[2:]]
-    e2e_mean = statistics.mean(e2e_ms)
+    e2e_serial_mean = statistics.mean(e2e_ms)
+    pipe_ms = []
+    for rep in range(2):  # the first pass warms the staging buffers
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        t0.synchronize()  # the region starts before the first copy is issued
+        T.stage_csr(hb_np, ha_np, ctx)
+        for i in range(k_e2e):
+            if i + 1 < k_e2e:
+                T.stage_csr(hb_np, ha_np, ctx)
+            flush.fill_(i)
+            r2 = T.count_csr(hb_np, ha_np, ctx=ctx, stream=stream.cuda_stream)
+            ok = ok and r2.triangles == expect_count
+        t1.record(stream)
+        torch.cuda.synchronize()
+        pipe_ms.append(t0.elapsed_time(t1) / k_e2e)
+    e2e_mean = pipe_ms[-1]
 
     if rank != 0:
         if dist:
@@ -358,7 +378,11 @@ def run_ours(args, ws, rank, local):
         "gpu_launches": int(launches),
         "e2e": {"value": m / (e2e_mean * 1e-3) / 1e9, "unit": "GTEPS",
                 "h2d_bytes_per_step": 8 * (n + 1) + 4 * m, "d2h_bytes_per_step": int(lib.trust_tc_readback_bytes()),
-                "ms_per_step": e2e_mean},
+                "ms_per_step": e2e_mean, "steps": k_e2e,
+                "mode": "pipelined: step i+1's H2D copy staged on the library's copy stream while step i "
+                        "is counted; L2 flushed before every count; region from before the first copy "
+                        "to after the last result read",
+                "serial": {"value": m / (e2e_serial_mean * 1e-3) / 1e9, "ms_per_step": e2e_serial_mean}},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": _traffic(args.workload), "peak_source": peak_src,
                      "algorithmic_bytes": algo_bytes,

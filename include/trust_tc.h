@@ -89,7 +89,8 @@ typedef struct trust_tc_opts {
 
 typedef struct trust_tc_result {
   uint64_t triangles;       /* the count                                                     */
-  double kernel_seconds;    /* CUDA-event time of classification + counting (validation excluded) */
+  double kernel_seconds;    /* CUDA-event time of classification + counting (validation too in
+                               a single-graph call, where it runs fused with classification) */
   double count_seconds;     /* CUDA-event time of the counting kernel alone                  */
   double call_seconds;      /* CUDA-event time of the whole device-side call                 */
   int64_t vertices;         /* n                                                            */
@@ -136,6 +137,16 @@ int trust_tc_validate_csr(const int64_t *begin, const int32_t *adj, int64_t n, i
  * memory inside the call.  ctx may be NULL (a temporary context is used). */
 int trust_tc_count_csr(trust_tc_ctx *ctx, const int64_t *begin, const int32_t *adj, int64_t n,
                        int64_t m, const trust_tc_opts *opts, trust_tc_result *result);
+
+/* Start copying a host CSR to the device on the context's own copy stream and return at once
+ * (no counterpart in the reference, whose host operator copies and counts in one blocking call,
+ * Without-graph-partition/TC.cu:640-696).  The next trust_tc_count_csr on this context with
+ * ptr_kind HOST and the same begin/adj pointers and n, m counts the staged copy (oldest first)
+ * instead of copying again, so a caller counting a stream of graphs overlaps the copy of the
+ * next one with the count of the current one.  Two staged inputs may wait at a time
+ * (TRUST_TC_E_ARG beyond that).  The host arrays must stay unchanged until the count that
+ * consumes them returns; with pinned memory the copy is asynchronous. */
+int trust_tc_stage_csr(trust_tc_ctx *ctx, const int64_t *begin, const int32_t *adj, int64_t n, int64_t m);
 
 /* Count over a device-resident CSR without allocating anything.  No counterpart in the
  * reference: it is for callers that may not allocate GPU memory while they count (memory owned

@@ -213,6 +213,29 @@ def test_host_input_validation_errors(ctx):
         assert e.value.status == _lib.E_OFFSETS
 
 
+@pytest.mark.parametrize("shift", [0, 1, 2, 3])
+def test_id_check_every_position_and_alignment(ctx, shift):
+    """The id check reads 16-byte words between scalar head and tail entries: a bad id is found
+    wherever it sits, whatever the alignment of the neighbour array (a view at an offset)."""
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "rmat_s12.npz"))
+    beg = np.asarray(z["ref_beg"], dtype=np.int64)
+    adj = np.asarray(z["ref_adj"], dtype=np.int32)
+    m, n = adj.size, beg.size - 1
+    expect = int(z["nx_triangles"][0])
+    big = torch.zeros(m + 8, dtype=torch.int32, device="cuda")
+    db = torch.from_numpy(beg).cuda()
+    for pos in sorted({0, 1, 2, 3, 4, 5, m // 2, m - 4, m - 3, m - 2, m - 1}):
+        for bad in (n, -1):
+            a = adj.copy()
+            a[pos] = bad
+            big[shift:shift + m] = torch.from_numpy(a).cuda()
+            with pytest.raises(T.TrustTcError) as e:
+                T.count_csr(db, big[shift:shift + m], ctx=ctx)
+            assert e.value.status == _lib.E_IDS, (pos, bad)
+    big[shift:shift + m] = torch.from_numpy(adj).cuda()
+    assert T.count_csr(db, big[shift:shift + m], ctx=ctx).triangles == expect
+
+
 def test_device_validation_errors(ctx):
     db, da = _dev(np.array([0, 2, 3, 3]), np.array([1, 3, 2]))
     with pytest.raises(T.TrustTcError) as e:

@@ -147,6 +147,16 @@ def count_csr(beg, adj, *, ctx: Context | None = None, threads=0, blocks=0, chun
     return _result(r)
 
 
+def stage_csr(beg: np.ndarray, adj: np.ndarray, ctx: Context) -> None:
+    """Start the host-to-device copy of a host CSR on the context's copy stream; the next
+    count_csr(beg, adj, ctx=ctx) counts the staged copy.  The arrays (int64 / int32, contiguous,
+    ideally pinned) must stay alive and unchanged until that count returns."""
+    assert isinstance(beg, np.ndarray) and beg.dtype == np.int64 and beg.flags.c_contiguous
+    assert isinstance(adj, np.ndarray) and adj.dtype == np.int32 and adj.flags.c_contiguous
+    check(load().trust_tc_stage_csr(ctx.handle, beg.ctypes.data_as(C.c_void_p), adj.ctypes.data_as(C.c_void_p),
+                                    beg.size - 1, adj.size), "trust_tc_stage_csr")
+
+
 def count_folder(folder: str, threads=0, blocks=0, chunk=0) -> CountResult:
     o = _opts(threads, blocks, chunk)
     r = _lib.Result()

@@ -77,6 +77,7 @@ SIGNATURES = {
     "trust_tc_validate_csr": (C.c_int, [_P, _P, C.c_int64, C.c_int64, _I64P]),
     "trust_tc_count_csr": (C.c_int, [_P, _P, _P, C.c_int64, C.c_int64, C.POINTER(Opts), C.POINTER(Result)]),
     "trust_tc_count_csr_noalloc": (C.c_int, [_P, _P, C.c_int64, C.c_int64, C.POINTER(Opts), C.POINTER(Result)]),
+    "trust_tc_stage_csr": (C.c_int, [_P, _P, _P, C.c_int64, C.c_int64]),
     "trust_tc_load_folder": (C.c_int, [C.c_char_p, C.POINTER(_I64P), C.POINTER(_I32P), _I64P, _I64P]),
     "trust_tc_save_folder": (C.c_int, [C.c_char_p, _P, _P, C.c_int64, C.c_int64]),
     "trust_tc_free_host": (None, [_P]),

@@ -56,11 +56,24 @@ int ctx_init(trust_tc_ctx *c, int device) {
   TC_CUDA_TRY(cudaMallocHost(&c->h_plans, TC_PLAN_WORDS * sizeof(unsigned long long)));
   for (auto &ev : c->ev) TC_CUDA_TRY(cudaEventCreate(&ev));
   for (auto &ev : c->ev_split) TC_CUDA_TRY(cudaEventCreate(&ev));
+  for (auto &sl : c->staged) TC_CUDA_TRY(cudaEventCreateWithFlags(&sl.ready, cudaEventDisableTiming));
+  TC_CUDA_TRY(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
   return TRUST_TC_OK;
 }
 
 void ctx_release(trust_tc_ctx *c) {
   if (c->device >= 0) cudaSetDevice(c->device);
+  if (c->copy_stream) {  // staged copies still in flight finish before their buffers go
+    cudaStreamSynchronize(c->copy_stream);
+    cudaStreamDestroy(c->copy_stream);
+    c->copy_stream = nullptr;
+  }
+  for (auto &sl : c->staged) {
+    cudaFree(sl.d_beg);
+    cudaFree(sl.d_adj);
+    if (sl.ready) cudaEventDestroy(sl.ready);
+    sl = trust_tc_ctx::Staged();
+  }
   cudaFree(c->d_ctl);
   cudaFreeHost(c->h_ctl);
   cudaFreeHost(c->h_plans);
@@ -194,24 +207,36 @@ int count_device(trust_tc_ctx *c, const DevGraph3 &g, const trust_tc_opts &o, bo
   TcControl *ctl = c->d_ctl;
   TC_CUDA_TRY(cudaEventRecord(c->ev[0], st));
   TC_CUDA_TRY(cudaMemsetAsync(ctl, 0, sizeof(TcControl), st));
-  // 1. validation of every distinct CSR: offsets always, ids on request
-  const int64_t rowsA = g.rowmap ? g.rowsA : g.rows;
-  rc = launch_check(g.begA, g.adjA, rowsA, g.mA, g.boundA, check_ids, ctl, c->num_sms, st);
-  if (rc) return rc;
-  if (!same) {
-    rc = launch_check(g.begB, g.adjB, g.rows, g.mB, g.boundB, check_ids, ctl, c->num_sms, st);
-    if (rc) return rc;
-    if (g.begC != g.begA || g.adjC != g.adjA) {
-      rc = launch_check(g.begC, g.adjC, g.rowsC, g.mC, g.boundC, check_ids, ctl, c->num_sms, st);
-      if (rc) return rc;
-    }
-  }
-  // 2. classification histogram
-  TC_CUDA_TRY(cudaEventRecord(c->ev[1], st));
   ListOffsets off{};
-  rc = launch_classify(0, g.begA, g.begB, g.rows, g.min_deg, cfg.warp_max, cfg.cta_max, ctl, c->d_lists,
-                       off, c->num_sms, st, o.schedule, g.rowmap);
-  if (rc) return rc;
+  // one CSR: validation, class histogram and list scatter in one kernel, each class listed in a
+  // fixed range of the list buffer (7 rows entries), so no offsets wait for the host
+  const bool fused = same && !g.rowmap && 7 * g.rows < ((int64_t)1 << 31);
+  if (fused) {
+    rc = ensure((void **)&c->d_lists, &c->lists_cap, sizeof(int) * (size_t)std::max<int64_t>(7 * g.rows, 1));
+    if (rc) return rc;
+    TC_CUDA_TRY(cudaEventRecord(c->ev[1], st));
+    rc = launch_check_classify(g.begA, g.adjA, g.rows, g.mA, check_ids, g.min_deg, cfg.warp_max, cfg.cta_max,
+                               o.schedule, ctl, c->d_lists, c->num_sms, st);
+    if (rc) return rc;
+  } else {
+    // 1. validation of every distinct CSR: offsets always, ids on request
+    const int64_t rowsA = g.rowmap ? g.rowsA : g.rows;
+    rc = launch_check(g.begA, g.adjA, rowsA, g.mA, g.boundA, check_ids, ctl, c->num_sms, st);
+    if (rc) return rc;
+    if (!same) {
+      rc = launch_check(g.begB, g.adjB, g.rows, g.mB, g.boundB, check_ids, ctl, c->num_sms, st);
+      if (rc) return rc;
+      if (g.begC != g.begA || g.adjC != g.adjA) {
+        rc = launch_check(g.begC, g.adjC, g.rowsC, g.mC, g.boundC, check_ids, ctl, c->num_sms, st);
+        if (rc) return rc;
+      }
+    }
+    // 2. classification histogram
+    TC_CUDA_TRY(cudaEventRecord(c->ev[1], st));
+    rc = launch_classify(0, g.begA, g.begB, g.rows, g.min_deg, cfg.warp_max, cfg.cta_max, ctl, c->d_lists,
+                         off, c->num_sms, st, o.schedule, g.rowmap);
+    if (rc) return rc;
+  }
   TC_CUDA_TRY(cudaMemcpyAsync(c->h_ctl, ctl, sizeof(TcControl), cudaMemcpyDeviceToHost, st));
   TC_CUDA_TRY(cudaStreamSynchronize(st));
   TcControl h = *c->h_ctl;
@@ -287,13 +312,17 @@ int count_device(trust_tc_ctx *c, const DevGraph3 &g, const trust_tc_opts &o, bo
     split_plan_read(c, &plan);
     split = o.direction_split == 1 || split_pays(plan.w_all, plan.w_min, g.mB, g.rows);
   }
+  // the fused pass's lists stand unless the learned decisions re-classified the rows
+  const bool lists_done = fused && !dec;
   int64_t total = 0;
   for (int k = TC_CLASS_SKIP + 1; k < TC_NUM_CLASSES; ++k) {
-    off.off[k] = (int)total;
+    off.off[k] = lists_done ? (int)((k - 1) * g.rows) : (int)total;
     total += h.class_count[k];
   }
-  rc = ensure((void **)&c->d_lists, &c->lists_cap, (size_t)std::max<int64_t>(total, 1) * sizeof(int));
-  if (rc) return rc;
+  if (!lists_done) {
+    rc = ensure((void **)&c->d_lists, &c->lists_cap, (size_t)std::max<int64_t>(total, 1) * sizeof(int));
+    if (rc) return rc;
+  }
   CountArgs a{};
   // huge class: hub rows in shared memory - one CTA while the table fits in 64 KiB, above that a
   // thread-block cluster with the table split over its CTAs' shared memory (up to 8 CTAs, up to
@@ -346,9 +375,11 @@ int count_device(trust_tc_ctx *c, const DevGraph3 &g, const trust_tc_opts &o, bo
     if (rc) return rc;
   }
   // 3. scatter the class lists
-  rc = launch_classify(1, g.begA, g.begB, g.rows, g.min_deg, cfg.warp_max, cfg.cta_max, ctl, c->d_lists,
-                       off, c->num_sms, st, o.schedule, g.rowmap, dec);
-  if (rc) return rc;
+  if (!lists_done) {
+    rc = launch_classify(1, g.begA, g.begB, g.rows, g.min_deg, cfg.warp_max, cfg.cta_max, ctl, c->d_lists,
+                         off, c->num_sms, st, o.schedule, g.rowmap, dec);
+    if (rc) return rc;
+  }
   if (pred) {  // heaviest first inside the huge, CTA and warp queues
     rc = lpt_sort(c, c->d_lists, off.off, h.class_count, pred, st);
     if (rc) return rc;
@@ -613,14 +644,25 @@ int trust_tc_count_csr(trust_tc_ctx *ctx, const int64_t *beg, const int32_t *adj
   if ((rc = cuda_status(cudaSetDevice(c->device)))) { if (c == &tmp) ctx_release(&tmp); return rc; }
   DevGraph3 g{};
   bool check_ids = false;
+  trust_tc_ctx::Staged *slot = nullptr;
   if (o.ptr_kind == TRUST_TC_HOST) {
-    rc = ensure((void **)&c->d_beg, &c->beg_cap, sizeof(int64_t) * (size_t)(n + 1));
-    if (!rc) rc = ensure((void **)&c->d_adj, &c->adj_cap, sizeof(int32_t) * (size_t)std::max<int64_t>(m, 1));
     cudaStream_t st = (cudaStream_t)o.stream;
-    if (!rc) rc = cuda_status(cudaMemcpyAsync(c->d_beg, beg, sizeof(int64_t) * (size_t)(n + 1), cudaMemcpyHostToDevice, st));
-    if (!rc && m) rc = cuda_status(cudaMemcpyAsync(c->d_adj, adj, sizeof(int32_t) * (size_t)m, cudaMemcpyHostToDevice, st));
-    g.begA = g.begB = g.begC = c->d_beg;
-    g.adjA = g.adjB = g.adjC = c->d_adj;
+    // a copy staged ahead by trust_tc_stage_csr for these host buffers: the oldest one
+    for (auto &sl : c->staged)
+      if (sl.waiting && sl.h_beg == beg && sl.h_adj == adj && sl.n == n && sl.m == m && (!slot || sl.seq < slot->seq))
+        slot = &sl;
+    if (slot) {
+      rc = cuda_status(cudaStreamWaitEvent(st, slot->ready, 0));
+      g.begA = g.begB = g.begC = slot->d_beg;
+      g.adjA = g.adjB = g.adjC = slot->d_adj;
+    } else {
+      rc = ensure((void **)&c->d_beg, &c->beg_cap, sizeof(int64_t) * (size_t)(n + 1));
+      if (!rc) rc = ensure((void **)&c->d_adj, &c->adj_cap, sizeof(int32_t) * (size_t)std::max<int64_t>(m, 1));
+      if (!rc) rc = cuda_status(cudaMemcpyAsync(c->d_beg, beg, sizeof(int64_t) * (size_t)(n + 1), cudaMemcpyHostToDevice, st));
+      if (!rc && m) rc = cuda_status(cudaMemcpyAsync(c->d_adj, adj, sizeof(int32_t) * (size_t)m, cudaMemcpyHostToDevice, st));
+      g.begA = g.begB = g.begC = c->d_beg;
+      g.adjA = g.adjB = g.adjC = c->d_adj;
+    }
     check_ids = true;  // host input is checked on the device after the copy, never skipped
   } else {
     g.begA = g.begB = g.begC = beg;
@@ -634,10 +676,39 @@ int trust_tc_count_csr(trust_tc_ctx *ctx, const int64_t *beg, const int32_t *adj
     g.min_deg = 2;
     rc = count_device(c, g, o, check_ids, r);
   }
+  if (slot) {  // count_device has synchronised (or failed): the slot is free for the next stage
+    if (rc) cudaStreamSynchronize((cudaStream_t)o.stream);
+    slot->waiting = 0;
+  }
   r->vertices = n;
   r->edges = m;
   if (c == &tmp) ctx_release(&tmp);
   return rc;
+}
+
+int trust_tc_stage_csr(trust_tc_ctx *ctx, const int64_t *beg, const int32_t *adj, int64_t n, int64_t m) {
+  if (!ctx || !beg || n < 0 || m < 0 || (m > 0 && !adj)) return TRUST_TC_E_ARG;
+  if (n >= ((int64_t)1 << 31) || m >= ((int64_t)1 << 31)) return TRUST_TC_E_TOO_LARGE;
+  trust_tc_ctx::Staged *sl = nullptr;
+  for (auto &x : ctx->staged)
+    if (!x.waiting) { sl = &x; break; }
+  if (!sl) return TRUST_TC_E_ARG;  // two staged inputs are already waiting for their counts
+  int rc = cuda_status(cudaSetDevice(ctx->device));
+  if (rc) return rc;
+  if ((rc = ensure((void **)&sl->d_beg, &sl->beg_cap, sizeof(int64_t) * (size_t)(n + 1)))) return rc;
+  if ((rc = ensure((void **)&sl->d_adj, &sl->adj_cap, sizeof(int32_t) * (size_t)std::max<int64_t>(m, 1)))) return rc;
+  TC_CUDA_TRY(cudaMemcpyAsync(sl->d_beg, beg, sizeof(int64_t) * (size_t)(n + 1), cudaMemcpyHostToDevice,
+                              ctx->copy_stream));
+  if (m)
+    TC_CUDA_TRY(cudaMemcpyAsync(sl->d_adj, adj, sizeof(int32_t) * (size_t)m, cudaMemcpyHostToDevice, ctx->copy_stream));
+  TC_CUDA_TRY(cudaEventRecord(sl->ready, ctx->copy_stream));
+  sl->h_beg = beg;
+  sl->h_adj = adj;
+  sl->n = n;
+  sl->m = m;
+  sl->seq = ++ctx->stage_seq;
+  sl->waiting = 1;
+  return TRUST_TC_OK;
 }
 
 void trust_tc_free_host(void *p) { free(p); }

@@ -16,6 +16,9 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <map>
+#include <mutex>
+#include <tuple>
 
 #include <cooperative_groups.h>
 
@@ -263,6 +266,28 @@ __device__ __forceinline__ void probe_warp_flat(const int32_t *__restrict__ adjC
 // ------------------------------------------------------------------------------------------
 // validation / classification
 // ------------------------------------------------------------------------------------------
+// TC_DEV_BAD_IDS if any of adj[0, m) lies outside [0, bound) (bound < 2^31).  Grid-strided over
+// 16-byte loads, two in flight per thread, with scalar loads for the entries before the first
+// 16-byte boundary and after the last: a streaming pass limited by bandwidth, not by latency.
+__device__ __forceinline__ int ids_out_of_range(const int32_t *__restrict__ adj, int64_t m, int64_t bound,
+                                                int64_t tid, int64_t stride) {
+  const unsigned ub = (unsigned)bound;
+  unsigned any = 0;
+  const int64_t lead = (int64_t)(((16u - ((unsigned)(uintptr_t)adj & 15u)) & 15u) >> 2);
+  const int64_t head = lead < m ? lead : m;
+  if (tid < head) any |= (unsigned)tc_ld_nc(adj + tid) >= ub;
+  const int4 *v4 = reinterpret_cast<const int4 *>(adj + head);
+  const int64_t n4 = (m - head) >> 2;
+  for (int64_t i = tid; i < n4; i += 2 * stride) {
+    const int4 a = __ldg(v4 + i);
+    const int4 b = i + stride < n4 ? __ldg(v4 + i + stride) : make_int4(0, 0, 0, 0);
+    any |= ((unsigned)a.x >= ub) | ((unsigned)a.y >= ub) | ((unsigned)a.z >= ub) | ((unsigned)a.w >= ub) |
+           ((unsigned)b.x >= ub) | ((unsigned)b.y >= ub) | ((unsigned)b.z >= ub) | ((unsigned)b.w >= ub);
+  }
+  for (int64_t i = head + 4 * n4 + tid; i < m; i += stride) any |= (unsigned)tc_ld_nc(adj + i) >= ub;
+  return any ? TC_DEV_BAD_IDS : 0;
+}
+
 __global__ void check_kernel(const int64_t *__restrict__ beg, const int32_t *__restrict__ adj,
                              int64_t rows, int64_t m, int64_t id_bound, int check_ids,
                              TcControl *ctl) {
@@ -283,12 +308,7 @@ __global__ void check_kernel(const int64_t *__restrict__ beg, const int32_t *__r
   if (tid == 0) {
     if (tc_ld_nc(beg) != 0 || tc_ld_nc(beg + rows) != m) bad |= TC_DEV_BAD_OFFSETS;
   }
-  if (check_ids) {
-    for (int64_t i = tid; i < m; i += stride) {
-      int x = tc_ld_nc(adj + i);
-      if (x < 0 || (int64_t)x >= id_bound) bad |= TC_DEV_BAD_IDS;
-    }
-  }
+  if (check_ids) bad |= ids_out_of_range(adj, m, id_bound, tid, stride);
   bad = __reduce_or_sync(TC_FULL_MASK, bad);
   dmax = __reduce_max_sync(TC_FULL_MASK, dmax);
   if ((threadIdx.x & 31) == 0) {
@@ -358,6 +378,84 @@ __global__ void class_kernel(const int64_t *__restrict__ begA, const int64_t *__
     __syncthreads();
   }
   (void)lane;
+}
+
+// One CSR (A = B = C, no row map): validation, class histogram and scatter in one kernel.  Class
+// c's list is the fixed range [(c-1) rows, c rows) of `lists` (a class holds at most `rows`
+// vertices), so no offsets need to reach the host first.  A block owns TC_CC_ROWS consecutive
+// rows, TC_CC_PER of them per thread with all their offsets loaded up front: it counts its
+// classes in shared memory, reserves its share of every class list with one global atomic per
+// class, and scatters from the classes kept in registers.  Rows with bad offsets are flagged and
+// left out of every list.  The id check is a separate grid-strided stream over adj.
+constexpr int TC_CC_THREADS = 256;
+constexpr int TC_CC_PER = 8;
+constexpr int TC_CC_ROWS = TC_CC_THREADS * TC_CC_PER;
+
+__global__ void __launch_bounds__(TC_CC_THREADS) check_class_kernel(
+    const int64_t *__restrict__ beg, const int32_t *__restrict__ adj, int64_t rows, int64_t m, int check_ids,
+    int min_deg, int warp_max, int cta_max, int plain, TcControl *ctl, int *__restrict__ lists) {
+  __shared__ int s_hist[TC_NUM_CLASSES];
+  __shared__ int s_base[TC_NUM_CLASSES];
+  const unsigned lt = tc_lanemask_lt();
+  const int64_t r0 = (int64_t)blockIdx.x * TC_CC_ROWS;
+  int bad = 0, dmax = 0;
+  if (threadIdx.x < TC_NUM_CLASSES) s_hist[threadIdx.x] = 0;
+  long long lo[TC_CC_PER], hi[TC_CC_PER];
+#pragma unroll
+  for (int k = 0; k < TC_CC_PER; ++k) {
+    const int64_t v = r0 + k * TC_CC_THREADS + threadIdx.x;
+    lo[k] = v < rows ? tc_ld_nc(beg + v) : 0;
+    hi[k] = v < rows ? tc_ld_nc(beg + v + 1) : 0;
+  }
+  int cls[TC_CC_PER];
+#pragma unroll
+  for (int k = 0; k < TC_CC_PER; ++k) {
+    const int64_t v = r0 + k * TC_CC_THREADS + threadIdx.x;
+    int c = -1;
+    if (v < rows) {
+      if (hi[k] < lo[k] || lo[k] < 0 || hi[k] > m) {
+        bad |= TC_DEV_BAD_OFFSETS;
+      } else if (hi[k] - lo[k] >= (1ll << 26)) {
+        bad |= TC_DEV_TOO_LARGE;
+      } else {
+        const int d = (int)(hi[k] - lo[k]);
+        dmax = max(dmax, d);
+        c = classify(d, d, min_deg, warp_max, cta_max, plain);
+      }
+    }
+    cls[k] = c;
+  }
+  __syncthreads();  // s_hist cleared
+#pragma unroll
+  for (int k = 0; k < TC_CC_PER; ++k) {
+    const unsigned peers = __match_any_sync(TC_FULL_MASK, cls[k]);
+    if (cls[k] >= 0 && (peers & lt) == 0) atomicAdd(&s_hist[cls[k]], __popc(peers));
+  }
+  __syncthreads();
+  if (threadIdx.x < TC_NUM_CLASSES) {
+    s_base[threadIdx.x] = s_hist[threadIdx.x] ? atomicAdd(&ctl->class_count[threadIdx.x], s_hist[threadIdx.x]) : 0;
+    s_hist[threadIdx.x] = 0;  // from here on: this block's fill cursor per class
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < TC_CC_PER; ++k) {
+    const int c = cls[k];
+    const unsigned peers = __match_any_sync(TC_FULL_MASK, c);
+    int at = 0;
+    if (c > TC_CLASS_SKIP && (peers & lt) == 0) at = atomicAdd(&s_hist[c], __popc(peers));
+    at = __shfl_sync(TC_FULL_MASK, at, __ffs(peers) - 1);
+    if (c > TC_CLASS_SKIP)
+      lists[(int64_t)(c - 1) * rows + s_base[c] + at + __popc(peers & lt)] = (int)(r0 + k * TC_CC_THREADS + threadIdx.x);
+  }
+  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (tid == 0 && (tc_ld_nc(beg) != 0 || tc_ld_nc(beg + rows) != m)) bad |= TC_DEV_BAD_OFFSETS;
+  if (check_ids) bad |= ids_out_of_range(adj, m, rows, tid, (int64_t)gridDim.x * blockDim.x);
+  bad = __reduce_or_sync(TC_FULL_MASK, bad);
+  dmax = __reduce_max_sync(TC_FULL_MASK, dmax);
+  if ((threadIdx.x & 31) == 0) {
+    if (bad) atomicOr(&ctl->status, bad);
+    if (dmax) atomicMax(&ctl->max_out_degree, dmax);
+  }
 }
 
 // Batch classification: the key of a row is (size class of its graph, degree class), with the
@@ -996,6 +1094,36 @@ __global__ void __launch_bounds__(512, 1) hub_kernel(CountArgs p, int log2C, int
   if (lane == 0 && wedges) atomicAdd(&p.ctl->wedges, wedges);
 }
 
+// Kernel attributes live per device and function, and every set is a driver call (several per
+// counting call otherwise, on the host path between classification and the count launch).  Each
+// (device, function, attribute) remembers what it was last set to; the dynamic shared memory
+// limit only ever grows.  Occupancy results are memoised per (device, kernel, threads, bytes).
+// Every attribute of the count kernels is set through here.
+struct AttrCache {
+  std::mutex mu;
+  std::map<std::tuple<int, const void *, int>, int> val;
+  std::map<std::tuple<int, const void *, int, size_t>, int> occ;
+};
+static AttrCache &attr_cache() {
+  static AttrCache c;
+  return c;
+}
+
+static cudaError_t set_attr(const void *fn, cudaFuncAttribute a, int v, bool grow_only = false) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  AttrCache &c = attr_cache();
+  std::lock_guard<std::mutex> lk(c.mu);
+  const auto key = std::make_tuple(dev, fn, (int)a);
+  auto it = c.val.find(key);
+  if (it != c.val.end() && (it->second == v || (grow_only && it->second > v))) return cudaSuccess;
+  e = cudaFuncSetAttribute(fn, a, v);
+  if (e == cudaSuccess) c.val[key] = v;
+  else c.val.erase(key);
+  return e;
+}
+
 int launch_hub(bool same, const CountArgs &a, int max_log2, int log2C, int clusters, cudaStream_t st) {
   // table share + staging for one CTA's share of the longest row (plus alignment slack)
   const int share_log2 = max_log2 - log2C;
@@ -1015,10 +1143,10 @@ int launch_hub(bool same, const CountArgs &a, int max_log2, int log2C, int clust
   cfg.numAttrs = 1;
   cudaError_t e;
   if (same) {
-    e = cudaFuncSetAttribute(hub_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    e = set_attr((const void *)hub_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem, true);
     if (e == cudaSuccess) e = cudaLaunchKernelEx(&cfg, hub_kernel<true>, a, log2C, share_log2);
   } else {
-    e = cudaFuncSetAttribute(hub_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    e = set_attr((const void *)hub_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem, true);
     if (e == cudaSuccess) e = cudaLaunchKernelEx(&cfg, hub_kernel<false>, a, log2C, share_log2);
   }
   TC_CUDA_TRY(e);
@@ -1035,6 +1163,19 @@ int launch_check(const int64_t *beg, const int32_t *adj, int64_t rows, int64_t m
   int blocks = (int)std::min<int64_t>((work + 255) / 256, (int64_t)num_sms * 8);
   blocks = std::max(blocks, 1);
   check_kernel<<<blocks, 256, 0, st>>>(beg, adj, rows, m, id_bound, check_ids, ctl);
+  TC_NOTE_LAUNCH();
+  TC_CUDA_TRY(cudaGetLastError());
+  return TRUST_TC_OK;
+}
+
+int launch_check_classify(const int64_t *beg, const int32_t *adj, int64_t rows, int64_t m, int check_ids,
+                          int min_deg, int warp_max, int cta_max, int schedule, TcControl *ctl, int *lists,
+                          int num_sms, cudaStream_t st) {
+  // one block per TC_CC_ROWS rows (its id-check share shrinks as the grid grows)
+  const int64_t blocks = std::max<int64_t>(1, (rows + TC_CC_ROWS - 1) / TC_CC_ROWS);
+  if (blocks > 0x7fffffff) return TRUST_TC_E_TOO_LARGE;
+  check_class_kernel<<<(unsigned)blocks, TC_CC_THREADS, 0, st>>>(beg, adj, rows, m, check_ids, min_deg, warp_max,
+                                                                 cta_max, schedule == TRUST_TC_SCHED_PLAIN, ctl, lists);
   TC_NOTE_LAUNCH();
   TC_CUDA_TRY(cudaGetLastError());
   return TRUST_TC_OK;
@@ -1058,20 +1199,39 @@ int launch_classify(int pass, const int64_t *begA, const int64_t *begB, int64_t 
 }
 
 // The occupancy query honours the kernel's preferred carveout, which a previous call may have
-// set low (a graph needing little shared memory); reset it to the maximum first, or the query
-// (and so the grid) would be limited by the last graph's carveout.
+// set low (a graph needing little shared memory); it runs with the carveout at the maximum, or
+// the query (and so the grid) would be limited by the last graph's carveout.
 template <bool SAME, int MAXT, int MINB>
 static cudaError_t occupancy_of(int threads, size_t smem_bytes, int *blocks_per_sm) {
   cudaError_t e = cudaSuccess;
-  for (auto fn : {count_kernel<SAME, false, MAXT, MINB, false>, count_kernel<SAME, true, MAXT, MINB, false>,
-                  count_kernel<SAME, false, MAXT, MINB, SAME>}) {
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
-    if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
+  const void *fns[3] = {(const void *)count_kernel<SAME, false, MAXT, MINB, false>,
+                        (const void *)count_kernel<SAME, true, MAXT, MINB, false>,
+                        (const void *)count_kernel<SAME, false, MAXT, MINB, SAME>};
+  for (const void *fn : fns)
+    if (e == cudaSuccess) e = set_attr(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes, true);
+  if (e != cudaSuccess) return e;
+  int dev = 0;
+  if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+  const auto key = std::make_tuple(dev, fns[0], threads, smem_bytes);
+  {
+    AttrCache &c = attr_cache();
+    std::lock_guard<std::mutex> lk(c.mu);
+    auto it = c.occ.find(key);
+    if (it != c.occ.end()) {
+      *blocks_per_sm = it->second;
+      return cudaSuccess;
+    }
   }
+  for (const void *fn : fns)
+    if (e == cudaSuccess) e = set_attr(fn, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
   if (e == cudaSuccess)
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, count_kernel<SAME, false, MAXT, MINB, false>, threads,
                                                       smem_bytes);
+  if (e == cudaSuccess) {
+    AttrCache &c = attr_cache();
+    std::lock_guard<std::mutex> lk(c.mu);
+    c.occ[key] = *blocks_per_sm;
+  }
   return e;
 }
 
@@ -1090,9 +1250,10 @@ int count_kernel_occupancy(bool same, int threads, size_t smem_bytes, int *block
 template <bool SAME, int MAXT, int MINB>
 static cudaError_t carveout_of(int pct) {
   cudaError_t e = cudaSuccess;
-  for (auto fn : {count_kernel<SAME, false, MAXT, MINB, false>, count_kernel<SAME, true, MAXT, MINB, false>,
-                  count_kernel<SAME, false, MAXT, MINB, SAME>})
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, pct);
+  for (const void *fn : {(const void *)count_kernel<SAME, false, MAXT, MINB, false>,
+                         (const void *)count_kernel<SAME, true, MAXT, MINB, false>,
+                         (const void *)count_kernel<SAME, false, MAXT, MINB, SAME>})
+    if (e == cudaSuccess) e = set_attr(fn, cudaFuncAttributePreferredSharedMemoryCarveout, pct);
   return e;
 }
 

@@ -41,6 +41,11 @@ struct CountArgs {
 
 int launch_check(const int64_t *beg, const int32_t *adj, int64_t rows, int64_t m, int64_t id_bound,
                  int check_ids, TcControl *ctl, int num_sms, cudaStream_t st);
+// One CSR: validation + class histogram + scatter in one kernel; class c (>= 1) is listed at
+// lists[(c-1) rows ...] and class_count[c] is its size.  lists holds 7 rows entries.
+int launch_check_classify(const int64_t *beg, const int32_t *adj, int64_t rows, int64_t m, int check_ids,
+                          int min_deg, int warp_max, int cta_max, int schedule, TcControl *ctl, int *lists,
+                          int num_sms, cudaStream_t st);
 int launch_classify(int pass, const int64_t *begA, const int64_t *begB, int64_t rows, int min_deg,
                     int warp_max, int cta_max, TcControl *ctl, int *lists, const ListOffsets &off,
                     int num_sms, cudaStream_t st, int schedule = TRUST_TC_SCHED_TUNED,

@@ -59,6 +59,22 @@ struct trust_tc_ctx {
   size_t adj_cap = 0;
   cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   cudaEvent_t ev_split[2] = {nullptr, nullptr};
+  // host CSRs staged ahead of their count (trust_tc_stage_csr): copied on copy_stream into one of
+  // two slots, consumed oldest-first by the count call given the same host pointers and sizes
+  struct Staged {
+    int64_t *d_beg = nullptr;
+    size_t beg_cap = 0;
+    int32_t *d_adj = nullptr;
+    size_t adj_cap = 0;
+    const int64_t *h_beg = nullptr;
+    const int32_t *h_adj = nullptr;
+    int64_t n = 0, m = 0;
+    int waiting = 0;       // staged and not yet counted
+    uint64_t seq = 0;      // staging order
+    cudaEvent_t ready = nullptr;
+  } staged[2];
+  uint64_t stage_seq = 0;
+  cudaStream_t copy_stream = nullptr;
 };
 
 namespace tc {
