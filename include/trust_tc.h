@@ -242,7 +242,8 @@ int trust_tc_gen_er_device(trust_tc_ctx *ctx, int64_t n, int64_t npairs, uint64_
 
 /* Autotuner for one graph (device CSR, opts->ptr_kind = TRUST_TC_DEVICE): times the counting call
  * `repeats` times per candidate and keeps the fastest, by coordinate descent from `base` over
- * threads per CTA (128/256/512/1024), warp-class bound (64/128/256, and the default), queue chunk
+ * the schedule (learned / tuned / plain, the last winning on some small graphs), then threads
+ * per CTA (128/256/512/1024), warp-class bound (64/128/256, and the default), queue chunk
  * (4/8/16) and, when
  * the graph has rows above the CTA table, hub_cluster (0/1/2/4/-1).  *best receives the chosen
  * options (pass them to trust_tc_count_csr), *best_ms their median call time.  Every candidate

@@ -129,6 +129,7 @@ def test_autotune(ctx):
     expect = T.count_csr(beg, adj, ctx=ctx).triangles
     cfg, ms = T.autotune(beg, adj, ctx, repeats=2)
     assert ms > 0 and cfg["threads"] in (0, 128, 256, 512, 1024) and cfg["chunk"] in (0, 4, 8, 16)
+    assert cfg["schedule"] in (T.SCHED_LEARNED, T.SCHED_TUNED, T.SCHED_PLAIN)
     assert T.count_csr(beg, adj, ctx=ctx, **cfg).triangles == expect
     # a graph with a row above the CTA table: the hub cluster size is tuned too
     import torch

@@ -608,6 +608,10 @@ int trust_tc_autotune(trust_tc_ctx *ctx, const int64_t *beg, const int32_t *adj,
     }
     return TRUST_TC_OK;
   };
+  // the schedule first (the plain split can win on small graphs, where the longest rows bound
+  // the time), then the launch shape under it
+  if ((rc = sweep(&trust_tc_opts::schedule, {TRUST_TC_SCHED_LEARNED, TRUST_TC_SCHED_TUNED, TRUST_TC_SCHED_PLAIN})))
+    return rc;
   if ((rc = sweep(&trust_tc_opts::threads_per_block, {128, 256, 512, 1024}))) return rc;
   if ((rc = sweep(&trust_tc_opts::warp_max_degree, {64, 128, 256}))) return rc;
   if ((rc = sweep(&trust_tc_opts::chunk, {4, 8, 16}))) return rc;
