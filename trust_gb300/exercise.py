@@ -4,7 +4,8 @@
 
 Used to profile all kernels in one process (R-MAT 18 ef16 under the tuned, learned, forced-hub and
 cycle-recording schedules, a 20,000-entry hub row on a thread-block cluster, the 2x2 device tile
-loop, a 256-graph batch, one epoch of cost-model training, the generators and GPU preprocessing).
+loop with the direction split, a staged host count, a 256-graph batch, one epoch of cost-model
+training, the generators and GPU preprocessing).
 """
 import numpy as np
 import torch
@@ -22,7 +23,8 @@ D = 20_000
 hb = torch.from_numpy(np.concatenate([[0], D + np.arange(0, D + 1)]).astype(np.int64)).cuda()
 ha = np.concatenate([np.arange(1, D + 1), np.arange(2, D + 2)]).astype(np.int32); ha[-1] = 0
 r3 = T.count_csr(hb, torch.from_numpy(ha).cuda(), ctx=ctx)                            # hub kernel, 4-CTA cluster
-r4 = T.count_tiles(beg, adj, 2)                                                      # GPU partition + tile jobs
+r4 = T.count_tiles(beg, adj, 2, direction_split=1)                                   # GPU partition, tile checks,
+                                                                                     # tile split plan, tile jobs
 specs = B.batch_specs(256, 50, 5000, seed=11)
 bp, vb = B.gen_batch_pairs(specs); bb, ba, gv = B.build_batch(bp, vb)                 # ba_kernel, batch build
 bt = B.Batch(bb, ba, gv, ctx=ctx); c, rb = bt.run()                                  # batch class/offsets/count
@@ -33,6 +35,9 @@ d = torch.from_numpy(np.diff(beg.cpu().numpy())).cuda(); m = d >= 2
 x = f[m][:20000].contiguous(); y = torch.log2(1 + cyc[m][:20000].float()).contiguous()
 mod, loss = T.model_train(x, y, T.model_init(seed=1), epochs=1, batch=4096, lr=1e-3)  # mlp grad + adam
 T.model_predict(x, mod)                                                              # predict
-assert r0.triangles == r1.triangles == r2.triangles == r4.triangles and r3.triangles == D - 1
+hb_np, ha_np = beg.cpu().pin_memory().numpy(), adj.cpu().pin_memory().numpy()
+T.stage_csr(hb_np, ha_np, ctx)
+r5 = T.count_csr(hb_np, ha_np, ctx=ctx)                                              # staged host input
+assert r0.triangles == r1.triangles == r2.triangles == r4.triangles == r5.triangles and r3.triangles == D - 1
 assert int(c.sum()) == rb.triangles
 print("ok", r0.triangles, rb.triangles)
