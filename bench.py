@@ -173,6 +173,36 @@ def make_graph_gpu(w):
     return beg, adj, {"generate_ms": (t1 - t0) * 1e3, "preprocess_ms": (t2 - t1) * 1e3}
 
 
+def workload_pairs_cpu(w):
+    """The workload's generated pairs and id bound, from the CPU oracle's generators."""
+    from oracle import oracle as O
+    if w["kind"] == "chung_lu":
+        cdf = O.chung_lu_cdf(w["n"], w["gamma"], w["w_max"], w["target"])
+        return O.gen_weighted(cdf, w["npairs"], w["seed"]), w["n"]
+    return O.gen_rmat(w["scale"], w["ef"] << w["scale"], w["a"], w["b"], w["c"], w["seed"]), 1 << w["scale"]
+
+
+def reference_preprocess(pairs, budget_s: float = 8.0):
+    """The reference's CPU preprocessing of this path (Preprocess/fromDirectToUndirect.cpp then
+    Preprocess/preprocess_outdegree.cpp, single-threaded as the reference runs it), restated in the
+    oracle, timed on growing prefixes of the workload's pairs until one run takes `budget_s` / 4."""
+    from oracle import oracle as O
+    total = pairs.shape[0]
+    npairs = min(total, 1 << 20)
+    while True:
+        t0 = time.perf_counter()
+        k, edges = O.ref_undirect(pairs[:npairs])
+        O.ref_outdegree_csr(k, edges)
+        t = time.perf_counter() - t0
+        if t >= budget_s / 4 or npairs == total:
+            break
+        npairs = min(total, npairs * 4)
+    return {"kind": "port", "cores": 1, "pairs": int(npairs), "of_pairs": int(total), "seconds": t,
+            "mpairs_per_s": npairs / t / 1e6,
+            "sample": "prefix of the workload's generated pairs: undirect (compact ids, dedupe) + orient by "
+                      "degree + renumber + CSR, one thread"}
+
+
 def make_graph_cpu(w):
     """The same graph built by the CPU oracle (used by the reference arm: no product code on it)."""
     from oracle import oracle as O
@@ -191,13 +221,7 @@ def make_graph_cpu(w):
             arcs += a.size
             total += sp.npairs
         return np.concatenate(begs + [np.array([arcs], dtype=np.int64)]), np.concatenate(adjs)
-    if w["kind"] == "chung_lu":
-        cdf = O.chung_lu_cdf(w["n"], w["gamma"], w["w_max"], w["target"])
-        pairs = O.gen_weighted(cdf, w["npairs"], w["seed"])
-        bound = w["n"]
-    else:
-        pairs = O.gen_rmat(w["scale"], w["ef"] << w["scale"], w["a"], w["b"], w["c"], w["seed"])
-        bound = 1 << w["scale"]
+    pairs, bound = workload_pairs_cpu(w)
     return O.build_csr(pairs, bound)
 
 
@@ -217,7 +241,24 @@ def cpu_baseline(beg_np, adj_np, budget_s: float = 12.0):
     t = statistics.median(times)
     return {"value": m / t / 1e9, "unit": "GTEPS", "cores": threads, "kind": "port",
             "sample": f"whole graph, {len(times)} runs (median {t * 1e3:.1f} ms), forward intersection over "
-                      f"presorted rows, {threads} threads"}, count
+                      f"presorted rows, {threads} threads",
+            "single_core": single_core_counter(beg_np, adj_np)}, count
+
+
+def single_core_counter(beg_np, adj_np, budget_s: float = 3.0):
+    """The same counter on one core over growing vertex prefixes (GTEPS of the arcs covered)."""
+    from oracle import oracle as O
+    n = beg_np.size - 1
+    hi = max(1, n // 64)
+    while True:
+        t0 = time.perf_counter()
+        O.count_forward_sorted_range(beg_np, adj_np, 0, hi, 2, 1)
+        t = time.perf_counter() - t0
+        if t >= budget_s / 4 or hi == n:
+            break
+        hi = min(n, hi * 4)
+    arcs = int(beg_np[hi] - beg_np[0])
+    return {"gteps": arcs / t / 1e9, "cores": 1, "sample": f"vertices [0, {hi}) of {n} ({arcs} arcs), {t:.2f} s"}
 
 
 def run_ours(args, ws, rank, local):
@@ -564,13 +605,24 @@ def run_reference(args, ws, rank, local):
                                    f"intersection over presorted rows, {threads} threads"},
         "e2e": {"value": value, "unit": "GTEPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+    line["cpu_baseline"]["single_core"] = single_core_counter(beg, adj)
+    if w["kind"] != "batch":
+        pairs, _ = workload_pairs_cpu(w)
+        line["reference_preprocess"] = reference_preprocess(pairs)
+        del pairs
     if O.ref_kernel_available():
         flags, _ = O.trust_check(beg, adj)
         if flags == O.TRUST_EXACT:
-            runs = [O.ref_kernel_count(beg, adj, blocks=1024, chunk=1) for _ in range(3)]
-            ms = statistics.median(r[1] for r in runs)
-            line["reference_kernel_sm103a"] = {"gteps": m / (ms * 1e-3) / 1e9, "kernel_ms": ms, "count": runs[0][0],
-                                               "launch": "dynamic_assign<<<1024,1024>>> chunk 1 (README example)"}
+            try:
+                runs = [O.ref_kernel_count(beg, adj, blocks=1024, chunk=1) for _ in range(3)]
+            except OSError as e:  # no CUDA driver on this host
+                runs = None
+                line["reference_kernel_sm103a"] = {"unavailable": f"cannot load the CUDA driver: {e}"}
+            if runs:
+                ms = statistics.median(r[1] for r in runs)
+                line["reference_kernel_sm103a"] = {"gteps": m / (ms * 1e-3) / 1e9, "kernel_ms": ms,
+                                                   "count": runs[0][0],
+                                                   "launch": "dynamic_assign<<<1024,1024>>> chunk 1 (README example)"}
         else:
             line["reference_kernel_sm103a"] = {"unavailable": f"reference kernel not exact on this CSR (flags {flags})"}
     print(json.dumps(line), flush=True)
