@@ -83,3 +83,32 @@ def test_staged_bad_ids_are_rejected():
             T.count_csr(b.numpy(), a2.numpy(), ctx=ctx)
         b3, a3, e3 = _pinned("k150")  # the context stays usable
         assert T.count_csr(b3.numpy(), a3.numpy(), ctx=ctx).triangles == e3
+
+
+def test_contexts_on_concurrent_host_threads():
+    """Separate contexts used from several host threads at once (the ctypes calls release the
+    GIL): launch attributes and occupancy are cached process-wide, counts stay exact."""
+    import threading
+    names = ["rmat_s12", "chung_lu_3000", "k150", "er_200"]
+    gs = [_pinned(n) for n in names]
+    errors, results = [], {}
+
+    def work(i):
+        try:
+            b, a, e = gs[i % len(gs)]
+            with T.Context() as ctx:
+                for k in range(6):
+                    threads = (128, 256, 512, 1024)[k % 4]
+                    r = T.count_csr(b.numpy(), a.numpy(), ctx=ctx, threads=threads)
+                    if r.triangles != e:
+                        errors.append((i, k, r.triangles, e))
+            results[i] = True
+        except Exception as ex:  # surfaced below
+            errors.append((i, repr(ex)))
+
+    ts = [threading.Thread(target=work, args=(i,)) for i in range(8)]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    assert not errors and len(results) == 8
