@@ -63,6 +63,16 @@ int ctx_init(trust_tc_ctx *c, int device) {
 
 void ctx_release(trust_tc_ctx *c) {
   if (c->device >= 0) cudaSetDevice(c->device);
+  if (c->sub) {
+    ctx_release(c->sub);
+    delete c->sub;
+    c->sub = nullptr;
+  }
+  if (c->sub_stream) {
+    cudaStreamSynchronize(c->sub_stream);
+    cudaStreamDestroy(c->sub_stream);
+    c->sub_stream = nullptr;
+  }
   if (c->copy_stream) {  // staged copies still in flight finish before their buffers go
     cudaStreamSynchronize(c->copy_stream);
     cudaStreamDestroy(c->copy_stream);
@@ -89,7 +99,6 @@ void ctx_release(trust_tc_ctx *c) {
   cudaFree(c->d_split_plans);
   cudaFree(c->d_sched_long);
   cudaFree(c->d_split_pairs);
-  cudaFree(c->d_split_ranks);
   cudaFree(c->d_split_beg);
   cudaFree(c->d_split_cbase);
   cudaFree(c->d_split_cbeg);
@@ -195,6 +204,9 @@ static bool split_pays(unsigned long long w_all, unsigned long long w_min, int64
   return (double)w_min <= 0.8 * (double)w_all && saved >= 32.0 * (double)(m + n);
 }
 
+static int split_second_pass(trust_tc_ctx *c, const DevGraph3 &g, const trust_tc_opts &o, bool same,
+                             int64_t max_out_degree, trust_tc_result *rb, float *t_build);
+
 // The device-side counting call over three CSRs (A = tables, B = arcs, C = probe lists).
 // `check_*` select which CSRs get an id-range check on the device.
 int count_device(trust_tc_ctx *c, const DevGraph3 &g, const trust_tc_opts &o, bool check_ids,
@@ -279,6 +291,7 @@ int count_device(trust_tc_ctx *c, const DevGraph3 &g, const trust_tc_opts &o, bo
     TC_CUDA_TRY(cudaStreamSynchronize(st));
     SchedPlan plan{};
     split_plan_read(c, &plan);
+    if (plan.overflow) return TRUST_TC_E_DEVICE;
     if (d_model) memcpy(h.class_count, c->h_ctl->class_count, sizeof h.class_count);
     const bool sorted = !(c->h_ctl->status & TC_DEV_UNSORTED);
     if (o.direction_split == 0) {
@@ -310,6 +323,7 @@ int count_device(trust_tc_ctx *c, const DevGraph3 &g, const trust_tc_opts &o, bo
     TC_CUDA_TRY(cudaStreamSynchronize(st));
     SchedPlan plan{};
     split_plan_read(c, &plan);
+    if (plan.overflow) return TRUST_TC_E_DEVICE;
     split = o.direction_split == 1 || split_pays(plan.w_all, plan.w_min, g.mB, g.rows);
   }
   // the fused pass's lists stand unless the learned decisions re-classified the rows
@@ -416,6 +430,23 @@ int count_device(trust_tc_ctx *c, const DevGraph3 &g, const trust_tc_opts &o, bo
   if (rc) return rc;
   TC_CUDA_TRY(cudaEventRecord(c->ev[3], st));
   TC_CUDA_TRY(cudaMemcpyAsync(c->h_ctl, ctl, sizeof(TcControl), cudaMemcpyDeviceToHost, st));
+  trust_tc_result rb;
+  memset(&rb, 0, sizeof rb);
+  float t_build = 0;
+  if (split) {
+    // Second pass: arcs (v,u) with d(u) > d(v), hashed on u's row, streaming the sources' rows (a
+    // tile job: tables from C's rows, probe rows from A's).  It runs on the context's second stream
+    // with a second context's scratch while the first pass still counts: the scheduling pass's
+    // outputs it reads are complete (the host has read their totals), and it writes nothing the
+    // first pass reads.  Its in-list build and setup (host round trips included) hide under the
+    // first pass, and its CTAs take SMs as the first pass's tail drains.
+    rc = split_second_pass(c, g, o, same, h.max_out_degree, &rb, &t_build);
+    if (rc) {
+      cudaStreamSynchronize(st);
+      return rc;
+    }
+    TC_CUDA_TRY(cudaStreamWaitEvent(st, c->ev_split[2], 0));
+  }
   TC_CUDA_TRY(cudaEventRecord(c->ev[4], st));
   TC_CUDA_TRY(cudaStreamSynchronize(st));
   const TcControl done = *c->h_ctl;
@@ -424,24 +455,46 @@ int count_device(trust_tc_ctx *c, const DevGraph3 &g, const trust_tc_opts &o, bo
   TC_CUDA_TRY(cudaEventElapsedTime(&t_kernel, c->ev[1], c->ev[3]));
   TC_CUDA_TRY(cudaEventElapsedTime(&t_count, c->ev[2], c->ev[3]));
   TC_CUDA_TRY(cudaEventElapsedTime(&t_call, c->ev[0], c->ev[4]));
-  r->triangles = done.count;
-  r->wedges = (int64_t)done.wedges;
+  if (split) {  // classification to the end of whichever pass ends last
+    float t_end_b = 0;
+    TC_CUDA_TRY(cudaEventElapsedTime(&t_end_b, c->ev[1], c->ev_split[2]));
+    t_kernel = std::max(t_kernel, t_end_b);
+  }
+  r->triangles = done.count + rb.triangles;
+  r->wedges = (int64_t)done.wedges + rb.wedges;
   r->kernel_seconds = t_kernel * 1e-3;
-  r->count_seconds = t_count * 1e-3;
+  r->count_seconds = t_count * 1e-3 + rb.count_seconds;  // both passes' count kernels
   r->call_seconds = t_call * 1e-3;
   r->max_out_degree = done.max_out_degree;
   for (int k = 0; k < TC_NUM_CLASSES; ++k) r->class_sizes[k] = h.class_count[k];
   r->direction_split = split;
   r->split_saving_ms = saving_ms;
-  if (split) {
-    // second pass: arcs (v,u) with d(u) > d(v), hashed on u's row, streaming the sources' rows
-    // (a tile job: tables from C's rows, probe rows from A's)
+  return TRUST_TC_OK;
+}
+
+// The direction split's second pass (see count_device), on c->sub_stream with c->sub's scratch.
+// Records ev_split[0] / [1] around the in-list build and ev_split[2] at its end.
+static int split_second_pass(trust_tc_ctx *c, const DevGraph3 &g, const trust_tc_opts &o, bool same,
+                             int64_t max_out_degree, trust_tc_result *rb, float *t_build) {
+  int rc;
+  if (!c->sub_stream) TC_CUDA_TRY(cudaStreamCreateWithFlags(&c->sub_stream, cudaStreamNonBlocking));
+  if (!c->sub) {
+    c->sub = new trust_tc_ctx;
+    if ((rc = ctx_init(c->sub, c->device))) {
+      ctx_release(c->sub);
+      delete c->sub;
+      c->sub = nullptr;
+      return rc;
+    }
+  }
+  cudaStream_t sb = c->sub_stream;
+  {
     SplitRows sr{};
-    TC_CUDA_TRY(cudaEventRecord(c->ev_split[0], st));
-    rc = same ? split_build(c, g.begA, g.adjA, g.rows, g.mA, st, &sr)
-              : split_build(c, g.begC, g.adjC, g.rowsC, g.mB, st, &sr);
+    TC_CUDA_TRY(cudaEventRecord(c->ev_split[0], sb));
+    rc = same ? split_build(c, g.begA, g.adjA, g.rows, g.mA, sb, &sr)
+              : split_build(c, g.begC, g.adjC, g.rowsC, g.mB, sb, &sr);
     if (rc) return rc;
-    TC_CUDA_TRY(cudaEventRecord(c->ev_split[1], st));
+    TC_CUDA_TRY(cudaEventRecord(c->ev_split[1], sb));
     DevGraph3 gb = g;
     if (!same) {
       gb.begA = g.begC; gb.adjA = g.adjC; gb.mA = g.mC; gb.boundA = g.boundC;
@@ -457,21 +510,15 @@ int count_device(trust_tc_ctx *c, const DevGraph3 &g, const trust_tc_opts &o, bo
     gb.rows = sr.rows;
     gb.min_deg = 1;
     gb.split_ok = 0;
-    gb.max_deg_A = h.max_out_degree;  // tables are whole rows (of the graph, or of C), not in-list chunks
+    gb.max_deg_A = max_out_degree;  // tables are whole rows (of the graph, or of C), not in-list chunks
     trust_tc_opts ob = o;
     ob.schedule = TRUST_TC_SCHED_TUNED;
     ob.record_cycles = 0;
-    trust_tc_result rb;
-    memset(&rb, 0, sizeof rb);
-    rc = count_device(c, gb, ob, false, &rb);
+    ob.stream = sb;
+    rc = count_device(c->sub, gb, ob, false, rb);
     if (rc) return rc;
-    float t_build = 0;
-    TC_CUDA_TRY(cudaEventElapsedTime(&t_build, c->ev_split[0], c->ev_split[1]));
-    r->triangles += rb.triangles;
-    r->wedges += rb.wedges;
-    r->kernel_seconds += rb.kernel_seconds + t_build * 1e-3;
-    r->count_seconds += rb.count_seconds;
-    r->call_seconds += rb.call_seconds + t_build * 1e-3;
+    TC_CUDA_TRY(cudaEventRecord(c->ev_split[2], sb));
+    TC_CUDA_TRY(cudaEventElapsedTime(t_build, c->ev_split[0], c->ev_split[1]));
   }
   return TRUST_TC_OK;
 }

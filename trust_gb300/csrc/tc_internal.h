@@ -39,8 +39,6 @@ struct trust_tc_ctx {
   unsigned long long *h_plans = nullptr;        // pinned host copy of d_split_plans
   int2 *d_split_pairs = nullptr;  // scheduling pass: the arcs the split would move, (target, source)
   size_t split_pairs_cap = 0;
-  unsigned *d_split_ranks = nullptr;  // and each one's slot in its target's in-list
-  size_t split_ranks_cap = 0;
   int *d_sched_long = nullptr;  // scheduling pass: the rows it walks a warp each
   size_t sched_long_cap = 0;
   int64_t *d_split_beg = nullptr;  // in-list offsets of the arcs sent to the second pass
@@ -58,7 +56,11 @@ struct trust_tc_ctx {
   int32_t *d_adj = nullptr;
   size_t adj_cap = 0;
   cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
-  cudaEvent_t ev_split[2] = {nullptr, nullptr};
+  cudaEvent_t ev_split[3] = {nullptr, nullptr, nullptr};
+  // the direction split's second pass runs on its own stream with its own scratch (a context of its
+  // own, made on first use) while the first pass still counts
+  trust_tc_ctx *sub = nullptr;
+  cudaStream_t sub_stream = nullptr;
   // host CSRs staged ahead of their count (trust_tc_stage_csr): copied on copy_stream into one of
   // two slots, consumed oldest-first by the count call given the same host pointers and sizes
   struct Staged {
@@ -114,7 +116,8 @@ struct SchedPlan {
   unsigned long long w_all, w_min;  // probes without / with the direction split
   float saved_cycles;               // model: predicted cycles the split saves on rows > 32
   int64_t long_rows;                // rows longer than 32 entries
-  int64_t moved_arcs;               // arcs the split sends to the second pass
+  int64_t moved_arcs;               // pair slots the pass used (moved arcs and holes)
+  bool overflow;                    // the pair arrays ran out (never expected): no split
 };
 int split_plan(trust_tc_ctx *c, const int64_t *beg, const int32_t *adj, int64_t n, int64_t m, cudaStream_t st,
                const float *d_model, int warp_max, int cta_max, float promote_log2, int cta_warps, TcControl *ctl);

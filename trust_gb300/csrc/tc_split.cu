@@ -134,48 +134,83 @@ __device__ __forceinline__ void long_row_arcs(const int64_t *__restrict__ beg, c
   }
 }
 
+// Pair slots are reserved TC_PAIR_BLOCK at a time per warp (one atomic on the shared slot counter
+// per block, not one per 32-arc step: every warp of the pass hits that counter).  A warp abandons
+// the rest of a block when a step's pairs do not fit, and at its end; abandoned slots are holes
+// (x = -1) that the fill skips.  Slots used <= moved arcs * TC_PAIR_BLOCK / (TC_PAIR_BLOCK - 31)
+// + TC_PAIR_BLOCK per warp (pair_slots() below).
+constexpr unsigned TC_PAIR_BLOCK = 256;
+struct PairBuf {
+  unsigned long long next = 0;  // warp-uniform: next free slot of the current block
+  unsigned avail = 0;           // slots left in it
+  unsigned long long cap;       // slots in the pair arrays; 0 once a reservation would pass them
+  unsigned long long *overflow; // set (never expected: the arrays hold pair_slots()) and no more pairs
+};
+
+__device__ __forceinline__ void pair_holes(PairBuf &pb, int2 *__restrict__ pairs) {
+  for (unsigned i = threadIdx.x & 31; i < pb.avail; i += 32) pairs[pb.next + i].x = -1;
+  pb.next += pb.avail;
+  pb.avail = 0;
+}
+
 // An arc (v,u) the split would move (mv): count it in u's in-list (cnt) and work sum (wsum) and
-// append it as a (target, source) pair with its slot in u's in-list (the rank the count returns),
-// so the in-lists are later filled without atomics.  Called by all 32 lanes together; lanes that
-// move an arc to the same target share one atomic (hub targets receive many).
+// append it as a (target, source) pair; the fill gives each pair its slot in u's in-list.  The
+// counts are reductions whose result nobody waits for, so a step of the pass never stalls on an
+// atomic's round trip.  Called by all 32 lanes together; lanes that move an arc to the same target
+// share one atomic (hub targets receive many).
 __device__ __forceinline__ void move_arc(bool mv, int u, int v, int dv, unsigned *__restrict__ cnt,
                                          unsigned long long *__restrict__ wsum, int2 *__restrict__ pairs,
-                                         unsigned *__restrict__ ranks, unsigned long long *npairs) {
+                                         unsigned long long *npairs, PairBuf &pb) {
   const unsigned m = __ballot_sync(TC_FULL_MASK, mv);
   if (!m) return;
   const int lane = threadIdx.x & 31;
   const unsigned lt = tc_lanemask_lt();
   const unsigned peers = __match_any_sync(TC_FULL_MASK, mv ? u : -1);
-  unsigned rank = 0;
   if (mv) {
-    const int leader = __ffs(peers) - 1;
     const unsigned sum = __reduce_add_sync(peers, (unsigned)dv);
-    unsigned base = 0;
-    if (lane == leader) {
-      base = atomicAdd(cnt + u, (unsigned)__popc(peers));
+    if ((peers & lt) == 0) {  // the group's leader
+      atomicAdd(cnt + u, (unsigned)__popc(peers));
       atomicAdd(wsum + u, (unsigned long long)sum);
     }
-    base = __shfl_sync(peers, base, leader);
-    rank = base + __popc(peers & lt);
   }
-  unsigned long long at = 0;
-  if (lane == 0) at = atomicAdd(npairs, (unsigned long long)__popc(m));
-  at = __shfl_sync(TC_FULL_MASK, at, 0);
-  if (mv) {
-    const unsigned long long k = at + __popc(m & lt);
-    pairs[k] = make_int2(u, v);
-    ranks[k] = rank;
+  const unsigned k = __popc(m);
+  if (pb.cap == 0) return;
+  if (k > pb.avail) {  // warp-uniform
+    pair_holes(pb, pairs);
+    unsigned long long at = 0;
+    if (lane == 0) at = atomicAdd(npairs, (unsigned long long)TC_PAIR_BLOCK);
+    at = __shfl_sync(TC_FULL_MASK, at, 0);
+    if (at + TC_PAIR_BLOCK > pb.cap) {
+      if (lane == 0) atomicOr(pb.overflow, 1ull);
+      pb.cap = 0;
+      return;
+    }
+    pb.next = at;
+    pb.avail = TC_PAIR_BLOCK;
   }
+  if (mv) pairs[pb.next + __popc(m & lt)] = make_int2(u, v);
+  pb.next += k;
+  pb.avail -= k;
 }
 
-// Fill the in-lists: every pair's source goes to its recorded slot.
-__global__ void split_fill_kernel(const int2 *__restrict__ pairs, const unsigned *__restrict__ ranks,
-                                  const unsigned long long *__restrict__ npairs, const int64_t *__restrict__ off,
+// Fill the in-lists: every pair's source goes to the next free slot of its target's in-list
+// (cursor: one counter per target, zeroed before), holes skipped; four pairs per thread in
+// flight, so the cursor atomics' round trips overlap.
+__global__ void split_fill_kernel(const int2 *__restrict__ pairs, const unsigned long long *__restrict__ npairs,
+                                  const int64_t *__restrict__ off, unsigned *__restrict__ cursor,
                                   int32_t *__restrict__ adj_b) {
   const int64_t np = (int64_t)*npairs;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < np; i += (int64_t)gridDim.x * blockDim.x) {
-    const int2 p = pairs[i];
-    adj_b[off[p.x] + ranks[i]] = p.y;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < np; i += 4 * stride) {
+    int2 p[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) p[r] = i + r * stride < np ? pairs[i + r * stride] : make_int2(-1, 0);
+    unsigned slot[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) slot[r] = p[r].x >= 0 ? atomicAdd(cursor + p[r].x, 1u) : 0u;
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+      if (p[r].x >= 0) adj_b[off[p[r].x] + slot[r]] = p[r].y;
   }
 }
 
@@ -232,7 +267,7 @@ __device__ __forceinline__ int tuned_class_of(int d, int warp_max, int cta_max) 
 }
 
 // Words of the scheduling pass's totals (plans[]).
-enum { PLAN_W_ALL = 0, PLAN_W_MIN = 1, PLAN_SAVED = 2, PLAN_NLONG = 3, PLAN_NPAIRS = 4 };
+enum { PLAN_W_ALL = 0, PLAN_W_MIN = 1, PLAN_SAVED = 2, PLAN_NLONG = 3, PLAN_NPAIRS = 4, PLAN_OVERFLOW = 5 };
 
 // The scheduling pass, phase 1 (rows of up to TC_SCHED_FLAT entries): the split plan's probe
 // totals, the in-list count and work sum of every arc's target, the arcs the split would move
@@ -240,10 +275,13 @@ enum { PLAN_W_ALL = 0, PLAN_W_MIN = 1, PLAN_SAVED = 2, PLAN_NLONG = 3, PLAN_NPAI
 __global__ void sched_short_kernel(const int64_t *__restrict__ beg, const int32_t *__restrict__ adj, int64_t n,
                                    unsigned *__restrict__ cnt, unsigned long long *__restrict__ wsum,
                                    unsigned long long *plans, int *__restrict__ longs, int2 *__restrict__ pairs,
-                                   unsigned *__restrict__ ranks, TcControl *ctl) {
+                                   unsigned long long pair_cap, TcControl *ctl) {
   const int lane = threadIdx.x & 31;
   unsigned long long w_all = 0, w_min = 0;
   int bad = 0;
+  PairBuf pb;
+  pb.cap = pair_cap;
+  pb.overflow = plans + PLAN_OVERFLOW;
   short_arcs(beg, adj, n, longs, plans + PLAN_NLONG,
              [&](bool valid, int v, int dv, int u, int du, int pos, bool last) {
                if (valid) {
@@ -251,8 +289,9 @@ __global__ void sched_short_kernel(const int64_t *__restrict__ beg, const int32_
                  w_min += (unsigned)min(du, dv);
                  if (!last) bad |= u >= tc_ld_nc(adj + pos + 1);
                }
-               move_arc(valid && du > dv, u, v, dv, cnt, wsum, pairs, ranks, plans + PLAN_NPAIRS);
+               move_arc(valid && du > dv, u, v, dv, cnt, wsum, pairs, plans + PLAN_NPAIRS, pb);
              });
+  pair_holes(pb, pairs);
 #pragma unroll
   for (int o = 16; o >= 1; o >>= 1) {
     w_all += __shfl_down_sync(TC_FULL_MASK, w_all, o);
@@ -276,7 +315,7 @@ __global__ void sched_long_kernel(const int64_t *__restrict__ beg, const int32_t
                                   unsigned long long *plans, const int *__restrict__ longs,
                                   const float *__restrict__ model, int warp_max, int cta_max, float promote_log2,
                                   unsigned char *__restrict__ dec, float *__restrict__ pred, float *sums,
-                                  int cta_warps, int2 *__restrict__ pairs, unsigned *__restrict__ ranks,
+                                  int cta_warps, int2 *__restrict__ pairs, unsigned long long pair_cap,
                                   TcControl *ctl) {
   __shared__ float P[MODEL ? TC_MODEL_FLOATS : 1];
   if (MODEL) {  // staged with W1 and W2 transposed (see warp_mlp)
@@ -301,6 +340,9 @@ __global__ void sched_long_kernel(const int64_t *__restrict__ beg, const int32_t
   unsigned long long w_all = 0, w_min = 0;
   float saved = 0.f;
   int bad = 0;
+  PairBuf pb;
+  pb.cap = pair_cap;
+  pb.overflow = plans + PLAN_OVERFLOW;
   for (int64_t idx = warp; idx < nl; idx += nwarps) {
     const int v = longs[idx];
     const long long lo = tc_ld_nc(beg + v);
@@ -316,7 +358,7 @@ __global__ void sched_long_kernel(const int64_t *__restrict__ beg, const int32_t
         rnb += mv;
         if (!last) bad |= u >= tc_ld_nc(adj + pos + 1);
       }
-      move_arc(mv, u, v, dv, cnt, wsum, pairs, ranks, plans + PLAN_NPAIRS);
+      move_arc(mv, u, v, dv, cnt, wsum, pairs, plans + PLAN_NPAIRS, pb);
     });
 #pragma unroll
     for (int o = 16; o >= 1; o >>= 1) {
@@ -345,6 +387,7 @@ __global__ void sched_long_kernel(const int64_t *__restrict__ beg, const int32_t
       }
     }
   }
+  pair_holes(pb, pairs);
   bad = __reduce_or_sync(TC_FULL_MASK, bad);
   if (lane == 0) {
     if (w_all) atomicAdd(plans + PLAN_W_ALL, w_all);
@@ -400,6 +443,13 @@ static int arc_blocks(int64_t n, int num_sms) {  // one warp per 32 vertices
   return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)num_sms * 16));
 }
 
+// Pair slots for `arcs` arcs traversed by `warps` warps: a warp gives up a block only when fewer
+// than 32 of its slots are left, so every block but a warp's last holds >= TC_PAIR_BLOCK - 31
+// pairs: slots <= moved * 256 / 225 + 256 per warp <= arcs + arcs / 7 + 256 (warps + 1).
+static size_t pair_slots(int64_t arcs, int64_t warps) {
+  return (size_t)(arcs + arcs / 7) + (size_t)TC_PAIR_BLOCK * (size_t)(warps + 1);
+}
+
 // The scheduling pass (one traversal of the arcs, two phases): probe totals of both plans, the
 // split's in-degree counts and work sums, the sortedness check (TC_DEV_UNSORTED in ctl), the list
 // of rows longer than TC_SCHED_FLAT (kept for split_build), and - with a model - every long row's
@@ -414,10 +464,9 @@ int split_plan(trust_tc_ctx *c, const int64_t *beg, const int32_t *adj, int64_t 
     return rc;
   if ((rc = ensure((void **)&c->d_split_wsum, &c->split_wsum_cap, sizeof(unsigned long long) * nn))) return rc;
   if ((rc = ensure((void **)&c->d_sched_long, &c->sched_long_cap, sizeof(int) * nn))) return rc;
-  if ((rc = ensure((void **)&c->d_split_pairs, &c->split_pairs_cap, sizeof(int2) * (size_t)std::max<int64_t>(m, 1))))
-    return rc;
-  if ((rc = ensure((void **)&c->d_split_ranks, &c->split_ranks_cap, sizeof(unsigned) * (size_t)std::max<int64_t>(m, 1))))
-    return rc;
+  const int sb = arc_blocks(n, c->num_sms), lb = c->num_sms * 8;  // 256-thread blocks of the two phases
+  const size_t slots = pair_slots(m, (int64_t)(sb + lb) * 8);
+  if ((rc = ensure((void **)&c->d_split_pairs, &c->split_pairs_cap, sizeof(int2) * slots))) return rc;
   if (d_model) {
     if ((rc = ensure((void **)&c->d_dec, &c->dec_cap, nn))) return rc;
     if ((rc = ensure((void **)&c->d_pred, &c->pred_cap, sizeof(float) * nn))) return rc;
@@ -426,20 +475,18 @@ int split_plan(trust_tc_ctx *c, const int64_t *beg, const int32_t *adj, int64_t 
   TC_CUDA_TRY(cudaMemsetAsync(c->d_split_wsum, 0, sizeof(unsigned long long) * (size_t)(n + 1), st));
   TC_CUDA_TRY(cudaMemsetAsync(c->d_split_plans, 0, TC_PLAN_WORDS * sizeof(unsigned long long), st));
   float *sums = reinterpret_cast<float *>(c->d_split_plans + PLAN_SAVED);
-  sched_short_kernel<<<arc_blocks(n, c->num_sms), 256, 0, st>>>(beg, adj, n, c->d_split_cnt, c->d_split_wsum,
-                                                                c->d_split_plans, c->d_sched_long, c->d_split_pairs,
-                                                                c->d_split_ranks, ctl);
+  sched_short_kernel<<<sb, 256, 0, st>>>(beg, adj, n, c->d_split_cnt, c->d_split_wsum, c->d_split_plans,
+                                         c->d_sched_long, c->d_split_pairs, slots, ctl);
   TC_NOTE_LAUNCH();
   TC_CUDA_TRY(cudaGetLastError());
-  const int lb = c->num_sms * 8;
   if (d_model)
     sched_long_kernel<true><<<lb, 256, 0, st>>>(beg, adj, c->d_split_cnt, c->d_split_wsum, c->d_split_plans,
                                                 c->d_sched_long, d_model, warp_max, cta_max, promote_log2, c->d_dec,
-                                                c->d_pred, sums, cta_warps, c->d_split_pairs, c->d_split_ranks, ctl);
+                                                c->d_pred, sums, cta_warps, c->d_split_pairs, slots, ctl);
   else
     sched_long_kernel<false><<<lb, 256, 0, st>>>(beg, adj, c->d_split_cnt, c->d_split_wsum, c->d_split_plans,
                                                  c->d_sched_long, nullptr, warp_max, cta_max, promote_log2, nullptr,
-                                                 nullptr, nullptr, cta_warps, c->d_split_pairs, c->d_split_ranks, ctl);
+                                                 nullptr, nullptr, cta_warps, c->d_split_pairs, slots, ctl);
   TC_NOTE_LAUNCH();
   TC_CUDA_TRY(cudaGetLastError());
   TC_CUDA_TRY(cudaMemcpyAsync(c->h_plans, c->d_split_plans, TC_PLAN_WORDS * sizeof(unsigned long long),
@@ -454,7 +501,8 @@ void split_plan_read(const trust_tc_ctx *c, SchedPlan *plan) {
   memcpy(&saved, &c->h_plans[PLAN_SAVED], sizeof saved);
   plan->saved_cycles = saved;
   plan->long_rows = (int64_t)c->h_plans[PLAN_NLONG];
-  plan->moved_arcs = (int64_t)c->h_plans[PLAN_NPAIRS];
+  plan->moved_arcs = (int64_t)c->h_plans[PLAN_NPAIRS];  // pair slots used, holes included
+  plan->overflow = c->h_plans[PLAN_OVERFLOW] != 0;
 }
 
 // ---- tile jobs: three CSRs ---------------------------------------------------------------------
@@ -467,11 +515,14 @@ void split_plan_read(const trust_tc_ctx *c, SchedPlan *plan) {
 __global__ void tile_sched_kernel(const int64_t *__restrict__ begA, const int64_t *__restrict__ begB,
                                   const int32_t *__restrict__ adjB, const int64_t *__restrict__ begC, int64_t rows,
                                   unsigned *__restrict__ cnt, unsigned long long *__restrict__ wsum,
-                                  unsigned long long *plans, int2 *__restrict__ pairs, unsigned *__restrict__ ranks) {
+                                  unsigned long long *plans, int2 *__restrict__ pairs, unsigned long long pair_cap) {
   const int lane = threadIdx.x & 31;
   const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   unsigned long long w_all = 0, w_min = 0;
+  PairBuf pb;
+  pb.cap = pair_cap;
+  pb.overflow = plans + PLAN_OVERFLOW;
   for (int64_t v = warp; v < rows; v += nwarps) {
     const int dA = (int)(tc_ld_nc(begA + v + 1) - tc_ld_nc(begA + v));
     if (dA < 1) continue;
@@ -486,9 +537,10 @@ __global__ void tile_sched_kernel(const int64_t *__restrict__ begA, const int64_
         w_all += (unsigned)du;
         w_min += (unsigned)min(du, dA);
       }
-      move_arc(i < dB && du > dA, u, (int)v, dA, cnt, wsum, pairs, ranks, plans + PLAN_NPAIRS);
+      move_arc(i < dB && du > dA, u, (int)v, dA, cnt, wsum, pairs, plans + PLAN_NPAIRS, pb);
     }
   }
+  pair_holes(pb, pairs);
 #pragma unroll
   for (int o = 16; o >= 1; o >>= 1) {
     w_all += __shfl_down_sync(TC_FULL_MASK, w_all, o);
@@ -507,15 +559,14 @@ int tile_split_plan(trust_tc_ctx *c, const DevGraph3 &g, cudaStream_t st) {
   if ((rc = ensure((void **)&c->d_split_plans, &c->split_plans_cap, TC_PLAN_WORDS * sizeof(unsigned long long))))
     return rc;
   if ((rc = ensure((void **)&c->d_split_wsum, &c->split_wsum_cap, sizeof(unsigned long long) * nt))) return rc;
-  const size_t mb = (size_t)std::max<int64_t>(g.mB, 1);
-  if ((rc = ensure((void **)&c->d_split_pairs, &c->split_pairs_cap, sizeof(int2) * mb))) return rc;
-  if ((rc = ensure((void **)&c->d_split_ranks, &c->split_ranks_cap, sizeof(unsigned) * mb))) return rc;
+  const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((g.rows + 7) / 8, (int64_t)c->num_sms * 8));
+  const size_t slots = pair_slots(g.mB, (int64_t)blocks * 8);
+  if ((rc = ensure((void **)&c->d_split_pairs, &c->split_pairs_cap, sizeof(int2) * slots))) return rc;
   TC_CUDA_TRY(cudaMemsetAsync(c->d_split_cnt, 0, sizeof(unsigned) * nt, st));
   TC_CUDA_TRY(cudaMemsetAsync(c->d_split_wsum, 0, sizeof(unsigned long long) * nt, st));
   TC_CUDA_TRY(cudaMemsetAsync(c->d_split_plans, 0, TC_PLAN_WORDS * sizeof(unsigned long long), st));
-  const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((g.rows + 7) / 8, (int64_t)c->num_sms * 8));
   tile_sched_kernel<<<blocks, 256, 0, st>>>(g.begA, g.begB, g.adjB, g.begC, g.rows, c->d_split_cnt, c->d_split_wsum,
-                                            c->d_split_plans, c->d_split_pairs, c->d_split_ranks);
+                                            c->d_split_plans, c->d_split_pairs, slots);
   TC_NOTE_LAUNCH();
   TC_CUDA_TRY(cudaGetLastError());
   TC_CUDA_TRY(cudaMemcpyAsync(c->h_plans, c->d_split_plans, TC_PLAN_WORDS * sizeof(unsigned long long),
@@ -582,10 +633,10 @@ int split_build(trust_tc_ctx *c, const int64_t *beg, const int32_t *adj, int64_t
   int64_t nchunks = 0;
   if ((rc = scan_exclusive_i64(c->d_split_cbase, c->d_split_cbase, n + 1, st, &nchunks))) return rc;
   if (nchunks > max_chunks) return TRUST_TC_E_DEVICE;
-  // scatter the sources
-  split_fill_kernel<<<arc_blocks(m, c->num_sms), 256, 0, st>>>(c->d_split_pairs, c->d_split_ranks,
-                                                               c->d_split_plans + PLAN_NPAIRS, c->d_split_beg,
-                                                               c->d_split_adj);
+  // scatter the sources; the in-degree counts (read by chunk_count_kernel above) become the cursors
+  TC_CUDA_TRY(cudaMemsetAsync(c->d_split_cnt, 0, sizeof(unsigned) * (size_t)(n + 1), st));
+  split_fill_kernel<<<arc_blocks(m, c->num_sms), 256, 0, st>>>(c->d_split_pairs, c->d_split_plans + PLAN_NPAIRS,
+                                                               c->d_split_beg, c->d_split_cnt, c->d_split_adj);
   TC_NOTE_LAUNCH();
   TC_CUDA_TRY(cudaGetLastError());
   chunk_fill_kernel<<<vb, 256, 0, st>>>(c->d_split_cbase, c->d_split_beg, n, total, nchunks, c->d_split_cbeg,
