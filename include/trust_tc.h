@@ -51,8 +51,9 @@ enum { TRUST_TC_HOST = 0, TRUST_TC_DEVICE = 1 };
 enum {
   TRUST_TC_SCHED_PLAIN = 0,   /* the reference's split: one warp per vertex for out-degree 2..100,
                                  one CTA above (USE_WARP / USE_CTA, Without-graph-partition/TC.cu:19-20) */
-  TRUST_TC_SCHED_LEARNED = 1, /* (default) TUNED classes; on graphs of at least 2^23 arcs with skewed
-                                 rows a scheduling pass runs a per-vertex cost model that promotes
+  TRUST_TC_SCHED_LEARNED = 1, /* (default) TUNED classes; on graphs of at least 2^22 arcs with at least
+                                 15 % of them in rows longer than 128 entries (skewed rows) a
+                                 scheduling pass runs a per-vertex cost model that promotes
                                  heavy vertices to CTA granularity, orders the warp, CTA and huge
                                  queues by predicted cost and decides the direction split from its
                                  predicted saving                                                    */

@@ -170,10 +170,15 @@ static int resolve_cfg(trust_tc_ctx *c, const trust_tc_opts &o, bool same, Launc
 // far longer than the rest of the queue).
 constexpr float TC_PROMOTE_LOG2 = 22.f;
 
-// Below this many arcs the learned schedule's scheduling pass (about 0.1-0.3 ms on GB300) cannot
-// be repaid: the whole count takes about 2 ms or less, and the measured split gain on R-MAT
-// scale 18 (3.8M arcs) is smaller than the pass.  Such graphs run the tuned schedule.
-constexpr int64_t TC_LEARNED_MIN_ARCS = (int64_t)1 << 23;
+// Below this many arcs the learned schedule's scheduling pass cannot be repaid: on R-MAT scale 18
+// (3.8M arcs, a 1.7 ms count) the split with the pass costs 2 % more than the tuned classes
+// without it, on scale 19 (7.7M arcs) it saves 5 %.  Smaller graphs run the tuned schedule.
+constexpr int64_t TC_LEARNED_MIN_ARCS = (int64_t)1 << 22;
+// Nor where few arcs sit in long rows: the split pays through the probes of rows longer than
+// TC_LONG_ROW (128) entries.  Measured on GB300: it paid on every R-MAT graph with a >= 0.57
+// (scales 18-21; 34-67 % of arcs in such rows) and lost on a = 0.45 R-MAT and Chung-Lu graphs
+// (0-6 %), where the pass alone cost 0.3-1.0 ms more than the tuned classes.
+constexpr double TC_LEARNED_MIN_LONG_FRAC = 0.15;
 
 // Make the cost model in use resident on the device: the caller's (opts.model) or the library's
 // default.  Sets *d_model to null when neither is available (no decisions from a model).
@@ -267,7 +272,8 @@ int count_device(trust_tc_ctx *c, const DevGraph3 &g, const trust_tc_opts &o, bo
   // graph large enough to repay it (it costs about two traversals of the arcs)
   const bool consider =
       same && g.min_deg == 2 && g.rows > 0 &&
-      (o.direction_split == 1 || (learned && h.max_out_degree >= 64 && g.mA >= TC_LEARNED_MIN_ARCS));
+      (o.direction_split == 1 || (learned && h.max_out_degree >= 64 && g.mA >= TC_LEARNED_MIN_ARCS &&
+                                  (!fused || (double)h.long_arcs >= TC_LEARNED_MIN_LONG_FRAC * (double)g.mA)));
   if (consider) {
     const float *d_model = nullptr;
     if (learned) {

@@ -45,7 +45,9 @@ struct TcControl {
   int class_cursor[TC_NUM_CLASSES];   // scatter cursors of the classification pass
   int class_next[TC_NUM_CLASSES];     // work-queue heads (atomic chunk claims)
   int class_off[TC_NUM_CLASSES];      // list offsets, when computed on the device (batches)
+  unsigned long long long_arcs;       // arcs of rows longer than TC_LONG_ROW (single-graph calls)
 };
+constexpr int TC_LONG_ROW = 128;
 
 #if defined(__CUDACC__)
 // Knuth multiplicative hash into a power-of-two table of 2^log2 slots.

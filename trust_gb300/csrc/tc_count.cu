@@ -399,6 +399,7 @@ __global__ void __launch_bounds__(TC_CC_THREADS) check_class_kernel(
   const unsigned lt = tc_lanemask_lt();
   const int64_t r0 = (int64_t)blockIdx.x * TC_CC_ROWS;
   int bad = 0, dmax = 0;
+  unsigned long long long_arcs = 0;
   if (threadIdx.x < TC_NUM_CLASSES) s_hist[threadIdx.x] = 0;
   long long lo[TC_CC_PER], hi[TC_CC_PER];
 #pragma unroll
@@ -420,6 +421,7 @@ __global__ void __launch_bounds__(TC_CC_THREADS) check_class_kernel(
       } else {
         const int d = (int)(hi[k] - lo[k]);
         dmax = max(dmax, d);
+        if (d > TC_LONG_ROW) long_arcs += (unsigned)d;
         c = classify(d, d, min_deg, warp_max, cta_max, plain);
       }
     }
@@ -452,9 +454,12 @@ __global__ void __launch_bounds__(TC_CC_THREADS) check_class_kernel(
   if (check_ids) bad |= ids_out_of_range(adj, m, rows, tid, (int64_t)gridDim.x * blockDim.x);
   bad = __reduce_or_sync(TC_FULL_MASK, bad);
   dmax = __reduce_max_sync(TC_FULL_MASK, dmax);
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) long_arcs += __shfl_down_sync(TC_FULL_MASK, long_arcs, o);
   if ((threadIdx.x & 31) == 0) {
     if (bad) atomicOr(&ctl->status, bad);
     if (dmax) atomicMax(&ctl->max_out_degree, dmax);
+    if (long_arcs) atomicAdd(&ctl->long_arcs, long_arcs);
   }
 }
 
