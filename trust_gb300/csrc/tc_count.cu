@@ -1176,8 +1176,9 @@ int launch_check(const int64_t *beg, const int32_t *adj, int64_t rows, int64_t m
 int launch_check_classify(const int64_t *beg, const int32_t *adj, int64_t rows, int64_t m, int check_ids,
                           int min_deg, int warp_max, int cta_max, int schedule, TcControl *ctl, int *lists,
                           int num_sms, cudaStream_t st) {
-  // one block per TC_CC_ROWS rows (its id-check share shrinks as the grid grows)
-  const int64_t blocks = std::max<int64_t>(1, (rows + TC_CC_ROWS - 1) / TC_CC_ROWS);
+  // one block per TC_CC_ROWS rows; blocks past the last row only check ids (few rows, many arcs)
+  int64_t blocks = std::max<int64_t>(1, (rows + TC_CC_ROWS - 1) / TC_CC_ROWS);
+  if (check_ids) blocks = std::max<int64_t>(blocks, std::min<int64_t>((m + 4095) / 4096, (int64_t)num_sms * 8));
   if (blocks > 0x7fffffff) return TRUST_TC_E_TOO_LARGE;
   check_class_kernel<<<(unsigned)blocks, TC_CC_THREADS, 0, st>>>(beg, adj, rows, m, check_ids, min_deg, warp_max,
                                                                  cta_max, schedule == TRUST_TC_SCHED_PLAIN, ctl, lists);

@@ -148,7 +148,7 @@ __global__ void rs_scatter_kernel(const u64 *__restrict__ in, u64 *__restrict__ 
   __shared__ u32 pre[NW][256];
   __shared__ u32 run[256];
   __shared__ u32 gbase[256];
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int tid = threadIdx.x, warp = tid >> 5;
   run[tid] = 0;
   gbase[tid] = offs[(size_t)tid * nblocks + blockIdx.x];
 #pragma unroll

@@ -608,7 +608,7 @@ int rows_increasing(trust_tc_ctx *c, const int64_t *beg, const int32_t *adj, int
 // Build the second pass's work rows (after split_plan, whose long-row list it reuses): the
 // in-list of every target, cut into chunks so one heavily targeted row spreads over many CTAs.
 // Outputs live in the context.
-int split_build(trust_tc_ctx *c, const int64_t *beg, const int32_t *adj, int64_t n, int64_t m, cudaStream_t st,
+int split_build(trust_tc_ctx *c, const int64_t *beg, const int32_t * /*adj*/, int64_t n, int64_t m, cudaStream_t st,
                 SplitRows *out) {
   const int64_t max_chunks = std::max<int64_t>(n, m) + 1;  // at most one chunk per source
   int rc;
