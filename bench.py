@@ -1,12 +1,12 @@
 """Benchmark: TEPS of the sm_103a hash triangle counter on one GB300 (replicas for N > 1).
 
-Workload (default): the Chung-Lu power-law graph with 3.8M vertices, degree exponent 2.5, maximum
-expected degree 800, ~16.5M undirected edges, seed 2 — the synthetic stand-in for the reference's
-Cit-Patents example (generated on the GPU, GPU-preprocessed to an oriented int32 CSR with int64
-offsets).  A step is one counting call over the whole graph.  Metric: TEPS = m / t, printed by the
-reference as GTEPS (Without-graph-partition/mpi_main.cpp:124), for the library's default (learned)
-schedule, with the plain degree-threshold schedule (the reference's USE_WARP/USE_CTA split) and
-the tuned classes measured in the same run.
+Workload (default): R-MAT scale 26, edge factor 32, (a,b,c,d) = (0.57,0.19,0.19,0.05), seed 3 — the
+skewed, largest single-GPU graph (2.15e9 generated pairs, 2.08e9 oriented arcs after dedupe;
+generated on the GPU, GPU-preprocessed to an oriented int32 CSR with int64 offsets).  A step is
+one counting call over the whole graph.  Metric: TEPS = m / t, printed by the reference as GTEPS
+(Without-graph-partition/mpi_main.cpp:115), for the library's default (learned) schedule, with the
+plain degree-threshold schedule (the reference's USE_WARP/USE_CTA split), the tuned classes and an
+autotuned launch measured in the same run, and the same graph counted as a 2x2 tile loop.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload NAME]
 
@@ -45,12 +45,15 @@ WORKLOADS = {
                         desc="R-MAT scale 24 edge factor 16 (0.70,0.125,0.125,0.05) seed=3 (cost model held out)"),
     "rmat26_ef32": dict(kind="rmat", scale=26, ef=32, a=0.57, b=0.19, c=0.19, seed=3, tiles=2,
                         desc="R-MAT scale 26 edge factor 32 (0.57,0.19,0.19,0.05) seed=3"),
+    "grid4096": dict(kind="grid", k=4096,
+                     desc="4096 x 4096 grid with one diagonal per cell (triangulated mesh; cost model held out)"),
     "batch4096": dict(kind="batch", graphs=4096, nmin=50, nmax=50_000, seed=5,
                       desc="4096 graphs, vertices log-uniform 50..50,000, alternately Erdos-Renyi (avg degree "
                            "4..64) and Barabasi-Albert (2..16 edges per vertex), seed=5"),
 }
-DEFAULT_WORKLOAD = "chung_lu_3.8m"
-L2_FLUSH_BYTES = 256 << 20  # > 126 MB L2; the default graph (~96 MB) fits in L2, so flush every step
+DEFAULT_WORKLOAD = "rmat26_ef32"
+L2_FLUSH_BYTES = 256 << 20  # > 126 MB L2: written before every timed step (small graphs fit in L2)
+BIG_ARCS = 1 << 28  # graphs this large take seconds per call: fewer repeats of the comparison runs
 METRIC = "TEPS on 1 GB300: learned/autotuned vs plain TRUST schedule; % HBM roofline"
 
 
@@ -161,6 +164,8 @@ def make_graph_gpu(w):
     if w["kind"] == "chung_lu":
         pairs = T.gen_chung_lu(w["n"], w["gamma"], w["w_max"], w["target"], w["npairs"], seed=w["seed"])
         bound = w["n"]
+    elif w["kind"] == "grid":
+        pairs, bound = grid_pairs_gpu(w["k"]), w["k"] * w["k"]
     else:
         pairs = T.gen_rmat(w["scale"], w["ef"], w["a"], w["b"], w["c"], seed=w["seed"])
         bound = 1 << w["scale"]
@@ -173,25 +178,58 @@ def make_graph_gpu(w):
     return beg, adj, {"generate_ms": (t1 - t0) * 1e3, "preprocess_ms": (t2 - t1) * 1e3}
 
 
-def workload_pairs_cpu(w):
-    """The workload's generated pairs and id bound, from the CPU oracle's generators."""
+def grid_pairs_gpu(k: int):
+    """The k x k grid with one diagonal per cell (right, down and down-right neighbours) as an
+    (npairs, 2) int32 CUDA tensor: 2 (k-1)^2 triangles."""
+    import torch
+    ids = torch.arange(k * k, dtype=torch.int32, device="cuda").view(k, k)
+    e = [torch.stack([ids[:, :-1].reshape(-1), ids[:, 1:].reshape(-1)], 1),
+         torch.stack([ids[:-1, :].reshape(-1), ids[1:, :].reshape(-1)], 1),
+         torch.stack([ids[:-1, :-1].reshape(-1), ids[1:, 1:].reshape(-1)], 1)]
+    return torch.cat(e).contiguous()
+
+
+def workload_npairs(w) -> int:
+    if w["kind"] == "chung_lu":
+        return w["npairs"]
+    if w["kind"] == "grid":
+        return 3 * w["k"] * (w["k"] - 1)
+    return w["ef"] << w["scale"]
+
+
+def workload_pairs_cpu(w, npairs: int | None = None):
+    """The first `npairs` (default all) of the workload's generated pairs and the id bound, from the
+    CPU oracle's generators (counter-based: a prefix is the same pairs as in the whole stream)."""
     from oracle import oracle as O
+    total = workload_npairs(w)
+    k = total if npairs is None else min(npairs, total)
     if w["kind"] == "chung_lu":
         cdf = O.chung_lu_cdf(w["n"], w["gamma"], w["w_max"], w["target"])
-        return O.gen_weighted(cdf, w["npairs"], w["seed"]), w["n"]
-    return O.gen_rmat(w["scale"], w["ef"] << w["scale"], w["a"], w["b"], w["c"], w["seed"]), 1 << w["scale"]
+        return O.gen_weighted(cdf, k, w["seed"]), w["n"]
+    if w["kind"] == "grid":
+        return grid_pairs_np(w["k"])[:k], w["k"] * w["k"]
+    return O.gen_rmat(w["scale"], k, w["a"], w["b"], w["c"], w["seed"]), 1 << w["scale"]
 
 
-def reference_preprocess(pairs, budget_s: float = 8.0):
+def grid_pairs_np(k: int):
+    import numpy as np
+    ids = np.arange(k * k, dtype=np.int32).reshape(k, k)
+    e = [np.stack([ids[:, :-1].ravel(), ids[:, 1:].ravel()], 1), np.stack([ids[:-1, :].ravel(), ids[1:, :].ravel()], 1),
+         np.stack([ids[:-1, :-1].ravel(), ids[1:, 1:].ravel()], 1)]
+    return np.concatenate(e).astype(np.int32)
+
+
+def reference_preprocess(w, budget_s: float = 8.0):
     """The reference's CPU preprocessing of this path (Preprocess/fromDirectToUndirect.cpp then
     Preprocess/preprocess_outdegree.cpp, single-threaded as the reference runs it), restated in the
     oracle, timed on growing prefixes of the workload's pairs until one run takes `budget_s` / 4."""
     from oracle import oracle as O
-    total = pairs.shape[0]
+    total = workload_npairs(w)
     npairs = min(total, 1 << 20)
     while True:
+        pairs, _ = workload_pairs_cpu(w, npairs)
         t0 = time.perf_counter()
-        k, edges = O.ref_undirect(pairs[:npairs])
+        k, edges = O.ref_undirect(pairs)
         O.ref_outdegree_csr(k, edges)
         t = time.perf_counter() - t0
         if t >= budget_s / 4 or npairs == total:
@@ -203,18 +241,34 @@ def reference_preprocess(pairs, budget_s: float = 8.0):
                       "degree + renumber + CSR, one thread"}
 
 
+def make_graph_reference(w):
+    """The workload's CSR for the reference arm, whose timed part is the CPU counter alone.  Built
+    by the CPU oracle pipeline where that takes seconds; R-MAT 26 (2.15e9 pairs, hours for the
+    single-threaded oracle pipeline) is built by the library's GPU preprocessing, outside the timed
+    region, which equals the oracle pipeline byte for byte wherever both are run (tests)."""
+    if workload_npairs(w) > (1 << 28) and w["kind"] != "batch":
+        import torch
+        torch.cuda.set_device(0)
+        beg, adj, _ = make_graph_gpu(w)
+        out = beg.cpu().numpy(), adj.cpu().numpy()
+        del beg, adj
+        torch.cuda.empty_cache()
+        return out, "library GPU preprocessing (untimed input build)"
+    return make_graph_cpu(w), "CPU oracle pipeline (untimed input build)"
+
+
 def make_graph_cpu(w):
-    """The same graph built by the CPU oracle (used by the reference arm: no product code on it)."""
+    """The same graph built by the CPU oracle (no product code on it)."""
     from oracle import oracle as O
     if w["kind"] == "batch":
         # the batch's first graphs, up to ~16M pairs, preprocessed one by one and concatenated
         import numpy as np
-        from trust_gb300.batch import batch_specs, oracle_graph_pairs
+        from trust_gb300.batch import batch_specs
         begs, adjs, base, arcs, total = [], [], 0, 0, 0
         for sp in batch_specs(w["graphs"], w["nmin"], w["nmax"], w["seed"]):
             if total >= 16_000_000:
                 break
-            b, a = O.build_csr(oracle_graph_pairs(sp), sp.n)
+            b, a = O.build_csr(O.batch_graph_pairs(sp.kind, sp.n, sp.param, sp.npairs, sp.seed), sp.n)
             begs.append(b[:-1] + arcs)
             adjs.append(a + base)
             base += b.size - 1
@@ -225,40 +279,61 @@ def make_graph_cpu(w):
     return O.build_csr(pairs, bound)
 
 
-def cpu_baseline(beg_np, adj_np, budget_s: float = 12.0):
-    """The oracle's forward-intersection counter on every host core over the whole graph (rows are
-    already sorted by the preprocessing, so no per-row sort is timed), repeated within a budget."""
+def sample_stride(beg_np, adj_np, threads: int, target_s: float, start_stride: int = 1 << 16):
+    """The smallest power-of-two row stride (from start_stride down to 1) at which one strided
+    sample of the oracle counter takes at least target_s: (stride, seconds, count, arcs)."""
+    from oracle import oracle as O
+    stride = start_stride
+    while True:
+        t0 = time.perf_counter()
+        c, arcs = O.count_forward_stride(beg_np, adj_np, 0, stride, 2, threads)
+        t = time.perf_counter() - t0
+        if t >= target_s or stride == 1:
+            return stride, t, c, arcs
+        stride = max(1, stride // 4 if t < target_s / 8 else stride // 2)
+
+
+def cpu_baseline(beg_np, adj_np, budget_s: float = 16.0):
+    """The oracle's forward-intersection counter on every host core (rows are already sorted by the
+    preprocessing, so no per-row sort is timed).  Small graphs: the whole graph, repeated within the
+    budget.  Large graphs: a systematic sample (every S-th source row, S a power of two chosen so a
+    sample takes about a quarter of the budget), so every degree class is represented; TEPS = the
+    sampled rows' arcs / time.  Returns (baseline, whole-graph count or None)."""
     from oracle import oracle as O
     threads = os.cpu_count() or 1
     n = beg_np.size - 1
     m = adj_np.size
-    times, count = [], None
+    stride, t, c, arcs = sample_stride(beg_np, adj_np, threads, budget_s / 4)
+    times, count = [t], (c if stride == 1 else None)
     t_start = time.perf_counter()
-    while len(times) < 5 and (time.perf_counter() - t_start) < budget_s:
+    while len(times) < 5 and (time.perf_counter() - t_start) < budget_s / 2:
         t0 = time.perf_counter()
-        count = O.count_forward_sorted_range(beg_np, adj_np, 0, n, 2, threads)
+        O.count_forward_stride(beg_np, adj_np, len(times) % stride, stride, 2, threads)
         times.append(time.perf_counter() - t0)
     t = statistics.median(times)
-    return {"value": m / t / 1e9, "unit": "GTEPS", "cores": threads, "kind": "port",
-            "sample": f"whole graph, {len(times)} runs (median {t * 1e3:.1f} ms), forward intersection over "
-                      f"presorted rows, {threads} threads",
+    sample = (f"whole graph, {len(times)} runs (median {t * 1e3:.1f} ms)" if stride == 1 else
+              f"every {stride}th source row ({arcs} of {m} arcs per sample), {len(times)} samples (median "
+              f"{t:.2f} s)")
+    return {"value": (m if stride == 1 else arcs) / t / 1e9, "unit": "GTEPS", "cores": threads, "kind": "port",
+            "sample": sample + f", forward intersection over presorted rows, {threads} threads",
             "single_core": single_core_counter(beg_np, adj_np)}, count
 
 
 def single_core_counter(beg_np, adj_np, budget_s: float = 3.0):
-    """The same counter on one core over growing vertex prefixes (GTEPS of the arcs covered)."""
-    from oracle import oracle as O
+    """The same counter on one core over a strided row sample (GTEPS of the arcs covered)."""
+    stride, t, _, arcs = sample_stride(beg_np, adj_np, 1, budget_s / 2, start_stride=1 << 20)
     n = beg_np.size - 1
-    hi = max(1, n // 64)
-    while True:
-        t0 = time.perf_counter()
-        O.count_forward_sorted_range(beg_np, adj_np, 0, hi, 2, 1)
-        t = time.perf_counter() - t0
-        if t >= budget_s / 4 or hi == n:
-            break
-        hi = min(n, hi * 4)
-    arcs = int(beg_np[hi] - beg_np[0])
-    return {"gteps": arcs / t / 1e9, "cores": 1, "sample": f"vertices [0, {hi}) of {n} ({arcs} arcs), {t:.2f} s"}
+    return {"gteps": arcs / t / 1e9, "cores": 1,
+            "sample": f"every {stride}th source row of {n} ({arcs} arcs), {t:.2f} s"}
+
+
+def pinned_count(workload):
+    """A whole-graph count of the workload pinned by a CPU oracle run (tests/golden/pinned_counts.json)."""
+    p = os.path.join(ROOT, "tests", "golden", "pinned_counts.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        return json.load(f).get(workload)
 
 
 def run_ours(args, ws, rank, local):
@@ -313,13 +388,17 @@ def run_ours(args, ws, rank, local):
     sched = {"learned": {"gteps": m / (statistics.median(step_ms) * 1e-3) / 1e9,
                          "ms": statistics.median(step_ms), "direction_split": res[0].direction_split,
                          "predicted_split_saving_ms": res[0].split_saving_ms}}
-    tuned_cfg, _ = T.autotune(beg, adj, ctx, repeats=3)  # outside every timed region
+    big = m >= BIG_ARCS  # a call takes seconds: bounded comparison runs and autotuner budget
+    t_tune = time.perf_counter()
+    tuned_cfg, _ = T.autotune(beg, adj, ctx, repeats=1 if big else 3,
+                              time_budget_s=24.0 if big else 0.0)  # outside every timed region
+    autotune_s = time.perf_counter() - t_tune
     runs = (("autotuned", lambda: T.count_csr(beg, adj, ctx=ctx, stream=stream.cuda_stream, **tuned_cfg)),
             ("tuned", lambda: call(T.SCHED_TUNED)), ("plain", lambda: call(T.SCHED_PLAIN)))
     for name, fn in runs:
         fn()
         ms = []
-        for i in range(max(5, args.steps // 10)):
+        for i in range(3 if big else max(5, args.steps // 10)):
             flush.fill_(i)
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             a.record(stream)
@@ -332,6 +411,7 @@ def run_ours(args, ws, rank, local):
                        "count_kernel_ms": r3.count_seconds * 1e3}
         if name == "autotuned":
             sched[name]["launch"] = tuned_cfg
+            sched[name]["autotune_s"] = autotune_s
 
     # the n x n tile loop on the same graph (once per mode, outside the timed region): tiles in HBM
     # under the learned and the plain schedule, and streamed through a 3.5-tile device budget
@@ -356,8 +436,9 @@ def run_ours(args, ws, rank, local):
     ha = adj.cpu().pin_memory()
     hb_np, ha_np = hb.numpy(), ha.numpy()
     e2e_ev = []
-    k_e2e = max(3, args.steps // 4)
-    for i in range(k_e2e + 2):
+    k_e2e = 3 if big else max(3, args.steps // 4)
+    warm_e2e = 1 if big else 2
+    for i in range(k_e2e + warm_e2e):
         flush.fill_(i)
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record(stream)
@@ -366,23 +447,24 @@ def run_ours(args, ws, rank, local):
         ok = ok and r2.triangles == expect_count
         e2e_ev.append((a, b))
     torch.cuda.synchronize()
-    e2e_ms = [a.elapsed_time(b) for a, b in e2e_ev[2:]]
+    e2e_ms = [a.elapsed_time(b) for a, b in e2e_ev[warm_e2e:]]
     e2e_serial_mean = statistics.mean(e2e_ms)
     pipe_ms = []
     for rep in range(2):  # the first pass warms the staging buffers
+        k_rep = (2 if big else k_e2e) if rep == 0 else k_e2e
         t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         t0.record(stream)
         t0.synchronize()  # the region starts before the first copy is issued
         T.stage_csr(hb_np, ha_np, ctx)
-        for i in range(k_e2e):
-            if i + 1 < k_e2e:
+        for i in range(k_rep):
+            if i + 1 < k_rep:
                 T.stage_csr(hb_np, ha_np, ctx)
             flush.fill_(i)
             r2 = T.count_csr(hb_np, ha_np, ctx=ctx, stream=stream.cuda_stream)
             ok = ok and r2.triangles == expect_count
         t1.record(stream)
         torch.cuda.synchronize()
-        pipe_ms.append(t0.elapsed_time(t1) / k_e2e)
+        pipe_ms.append(t0.elapsed_time(t1) / k_rep)
     e2e_mean = pipe_ms[-1]
 
     if rank != 0:
@@ -434,9 +516,14 @@ def run_ours(args, ws, rank, local):
     if tile_loop:
         line["tile_loop"] = tile_loop
     if ws == 1 and not args.no_cpu_baseline:
-        cb, cpu_count = cpu_baseline(beg.cpu().numpy(), adj.cpu().numpy())
+        cb, cpu_count = cpu_baseline(hb_np, ha_np)
         line["cpu_baseline"] = cb
-        line["count_matches_oracle"] = cpu_count == expect_count
+        if cpu_count is not None:
+            line["count_matches_oracle"] = cpu_count == expect_count
+    pinned = pinned_count(args.workload)
+    if pinned is not None:
+        line["count_matches_pinned"] = {"pinned": pinned["triangles"], "equal": pinned["triangles"] == expect_count,
+                                        "source": pinned["source"]}
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
@@ -608,48 +695,47 @@ def run_batch(args, ws, rank, local):
 
 def run_reference(args, ws, rank, local):
     """The reference's CPU-side counting for this path: it ships no CPU counter, so the oracle port of
-    its counted quantity runs on every host core, one bounded vertex slice per step.  Where the
-    reference kernel cubin is present (built from Without-graph-partition/TC.cu for sm_103a) its GPU
-    time on the same CSR is reported beside it."""
+    its counted quantity runs on every host core.  Each step counts a bounded systematic sample of
+    the workload (every S-th source row, the offset advancing per step; S = 1 on graphs whose whole
+    count takes about a second or less), so the whole run ends within minutes.  Where the reference
+    kernel cubin is present (built from Without-graph-partition/TC.cu for sm_103a) its GPU time on
+    the same CSR is reported beside it."""
     if rank != 0:
         return
-    import numpy as np
     from oracle import oracle as O
     w = WORKLOADS[args.workload]
-    beg, adj = make_graph_cpu(w)
+    if w["kind"] == "batch":
+        (beg, adj), how = make_graph_cpu(w), "CPU oracle pipeline (untimed input build)"
+    else:
+        (beg, adj), how = make_graph_reference(w)
     n, m = beg.size - 1, adj.size
     threads = os.cpu_count() or 1
-    slices = 8
-    bounds = np.linspace(0, n, slices + 1).astype(np.int64)
-    arcs = np.diff(beg[bounds])
+    stride, _, _, _ = sample_stride(beg, adj, threads, 1.5)
     for i in range(args.warmup):
-        s = i % slices
-        O.count_forward_sorted_range(beg, adj, int(bounds[s]), int(bounds[s + 1]), 2, threads)
+        O.count_forward_stride(beg, adj, i % stride, stride, 2, threads)
     tot_arcs, tot_t = 0, 0.0
     for i in range(args.steps):
-        s = i % slices
         t0 = time.perf_counter()
-        O.count_forward_sorted_range(beg, adj, int(bounds[s]), int(bounds[s + 1]), 2, threads)
+        _, arcs = O.count_forward_stride(beg, adj, (args.warmup + i) % stride, stride, 2, threads)
         tot_t += time.perf_counter() - t0
-        tot_arcs += int(arcs[s])
+        tot_arcs += arcs
     value = tot_arcs / tot_t / 1e9
+    sample = ("the whole graph per step" if stride == 1 else
+              f"every {stride}th source row per step (offset advancing per step, ~{m // stride} arcs)")
     line = {
         "impl": "reference",
         "metric": METRIC,
         "value": value, "unit": "GTEPS", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": tot_t / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded generator, CPU oracle pipeline)",
+        "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded generators); input CSR: " + how,
         "config": {"workload": w["desc"], "vertices": n, "edges": m, "schedule": "n/a: CPU forward intersection"},
         "cpu_baseline": {"value": value, "unit": "GTEPS", "cores": threads, "kind": "port",
-                         "sample": f"one of {slices} vertex slices per step (~{m // slices} arcs), forward "
-                                   f"intersection over presorted rows, {threads} threads"},
+                         "sample": sample + f", forward intersection over presorted rows, {threads} threads"},
         "e2e": {"value": value, "unit": "GTEPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     line["cpu_baseline"]["single_core"] = single_core_counter(beg, adj)
     if w["kind"] != "batch":
-        pairs, _ = workload_pairs_cpu(w)
-        line["reference_preprocess"] = reference_preprocess(pairs)
-        del pairs
+        line["reference_preprocess"] = reference_preprocess(w)
     if O.ref_kernel_available():
         flags, _ = O.trust_check(beg, adj)
         if flags == O.TRUST_EXACT:

@@ -86,6 +86,20 @@ typedef struct trust_tc_opts {
                             one CTA while the table fits in 64 KiB, else a thread-block cluster
                             with the table split over its CTAs (distributed shared memory);
                             1/2/4/8 = that cluster size; -1 = per-CTA global tables          */
+  int64_t row_begin;     /* trust_tc_count_csr / _folder: count only the arcs (v,u) whose source
+                            row v lies in [row_begin, row_end); row_end = 0 means n (the whole
+                            graph).  Every row is still validated and still serves as a probe
+                            row, and the schedule (classes, direction split) is decided the same
+                            way, so slices of a graph sum to its count.  Other entry points
+                            return TRUST_TC_E_UNSUPPORTED for a range.  No counterpart in the
+                            reference, whose ranks split the vertex chunks instead
+                            (Without-graph-partition/TC.cu:259, :433).                        */
+  int64_t row_end;
+  int test_wait_expiry;  /* test only (failure detection): 1 = the hub kernel arms its copy
+                            barrier without issuing the copy and waits a few thousand cycles, so
+                            the bounded wait runs out with nothing in flight; the kernel then
+                            reads the rows with plain loads and the call returns
+                            TRUST_TC_E_DEVICE with an exact count in the result.  0 in use.     */
 } trust_tc_opts;
 
 typedef struct trust_tc_result {
@@ -135,7 +149,9 @@ int trust_tc_validate_csr(const int64_t *begin, const int32_t *adj, int64_t n, i
 
 /* Count over a CSR.  Replaces dynamic_assign + its launch (Without-graph-partition/TC.cu:230-600,
  * :666-696).  Arrays are borrowed; with ptr_kind HOST they are copied to ctx-owned device
- * memory inside the call.  ctx may be NULL (a temporary context is used). */
+ * memory inside the call.  ctx may be NULL (a temporary context is used).  On TRUST_TC_E_DEVICE
+ * the result is filled as well: after an expired bounded wait the kernel re-read its rows with
+ * plain loads, so the count is exact; after a table overflow (never expected) it is not. */
 int trust_tc_count_csr(trust_tc_ctx *ctx, const int64_t *begin, const int32_t *adj, int64_t n,
                        int64_t m, const trust_tc_opts *opts, trust_tc_result *result);
 
@@ -155,9 +171,12 @@ int trust_tc_stage_csr(trust_tc_ctx *ctx, const int64_t *begin, const int32_t *a
  * stall other work).  Scratch comes from one 16 MiB array in the library's device image, held by
  * every GPU that loads the library until exit.  Limits: n <= 4,194,240 rows and every out-degree
  * within the CTA table (default 4096); larger inputs return TRUST_TC_E_TOO_LARGE.  opts->ptr_kind
- * must be TRUST_TC_DEVICE; timing fields of the result stay 0.  The first call on a device looks
- * up the array's address; make it before any stream capture.  Calls that overlap on the GPU race
- * on the shared array and must be serialised by the caller. */
+ * must be TRUST_TC_DEVICE and opts->record_cycles 0 (else TRUST_TC_E_UNSUPPORTED); timing fields
+ * of the result stay 0.  The first call on a device looks up the array's address and keeps it for
+ * the life of the process (not valid after cudaDeviceReset); make that first call before any
+ * stream capture.  Every call synchronises its stream twice and returns with the caller's current
+ * device unchanged.  Calls that overlap on the GPU race on the shared array and must be
+ * serialised by the caller. */
 int trust_tc_count_csr_noalloc(const int64_t *d_begin, const int32_t *d_adj, int64_t n, int64_t m,
                                const trust_tc_opts *opts, trust_tc_result *result);
 
@@ -248,10 +267,14 @@ int trust_tc_gen_er_device(trust_tc_ctx *ctx, int64_t n, int64_t npairs, uint64_
  * (4/8/16) and, when
  * the graph has rows above the CTA table, hub_cluster (0/1/2/4/-1).  *best receives the chosen
  * options (pass them to trust_tc_count_csr), *best_ms their median call time.  Every candidate
- * must give the same count (else TRUST_TC_E_DEVICE).  No counterpart in the reference, whose
- * threads/blocks/chunk come from argv (Without-graph-partition/mpi_main.cpp:84-88). */
+ * must give the same count (else TRUST_TC_E_DEVICE).  time_budget_s > 0 bounds the search: no new
+ * candidate starts once the calls made so far add up to that much time (0 = no bound; the
+ * candidates are tried in the order above, so a bound keeps the ones that matter most).  No
+ * counterpart in the reference, whose threads/blocks/chunk come from argv
+ * (Without-graph-partition/mpi_main.cpp:78-81). */
 int trust_tc_autotune(trust_tc_ctx *ctx, const int64_t *begin, const int32_t *adj, int64_t n, int64_t m,
-                      const trust_tc_opts *base, int repeats, trust_tc_opts *best, double *best_ms);
+                      const trust_tc_opts *base, int repeats, double time_budget_s, trust_tc_opts *best,
+                      double *best_ms);
 
 /* ---- batches: many graphs counted by one CUDA-graph launch -------------------------------
  * A batch is the disjoint union of many oriented graphs in one device CSR (ids global), graph g
@@ -261,7 +284,7 @@ int trust_tc_autotune(trust_tc_ctx *ctx, const int64_t *begin, const int32_t *ad
  * kernel with its own launch parameters; validation, classification, list offsets, the kernels
  * and the readback of the per-graph counts are captured in one CUDA graph at creation and
  * replayed by every run.  No counterpart in the reference, which counts one graph per run
- * (Without-graph-partition/mpi_main.cpp:90-124); the per-graph counts equal its counts. */
+ * (Without-graph-partition/mpi_main.cpp:75-119); the per-graph counts equal its counts. */
 #define TRUST_TC_BATCH_CLASSES 4
 typedef struct trust_tc_batch_class {
   int threads_per_block; /* 64..1024, multiple of 32 (default 256)                            */

@@ -3,11 +3,11 @@
  *
  * Declares the same `struct arguments` and `Triangle_count` as Without-graph-partition/TC.cuh:2-10
  * (C++ linkage), plus the partitioned overload of With-graph-partition/TC.cuh:10, so a non-MPI
- * main program written like Without-graph-partition/mpi_main.cpp:84-128 links against
+ * main program written like Without-graph-partition/mpi_main.cpp:75-119 links against
  * libtrust_tc.so unchanged.  Error behaviour matches the reference's HRR macro (Without-graph-partition/
  * herror.h:1-8): the message is printed and the process exits with EXIT_FAILURE.  Logical ranks:
  * the library counts on one GPU, so rank 0 returns the whole count and ranks > 0 return 0 (the
- * main program's SUM over ranks, mpi_main.cpp:119, is unchanged).
+ * main program's SUM over ranks, Without-graph-partition/mpi_main.cpp:110-112, is unchanged).
  */
 #ifndef TRUST_TC_SHIM_H
 #define TRUST_TC_SHIM_H

@@ -12,9 +12,10 @@
 #                                           sm_103a; loaded on the GPU host by ref_tc_driver.c
 #                                           (the x86 host binaries here do not run there)
 #
-# Usage: oracle/build_ref.sh [reference_root]   (default /root/reference)
+# Usage: oracle/build_ref.sh <reference_root>
 set -eu
-REF=${1:-/root/reference}
+[ $# -eq 1 ] || { echo "usage: $0 <reference_root>" >&2; exit 2; }
+REF=$1
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/_ref"
 mkdir -p "$OUT"

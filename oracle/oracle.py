@@ -30,6 +30,9 @@ def _declare(lib):
     lib.orc_count_forward_sorted_range.restype = C.c_int
     lib.orc_count_forward_sorted_range.argtypes = [_P, _P, C.c_int64, C.c_int64, C.c_int64, C.c_int, C.c_int,
                                                    C.POINTER(C.c_uint64)]
+    lib.orc_count_forward_stride.restype = C.c_int
+    lib.orc_count_forward_stride.argtypes = [_P, _P, C.c_int64, C.c_int64, C.c_int64, C.c_int, C.c_int,
+                                             C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
     lib.orc_wedges.restype = C.c_uint64
     lib.orc_wedges.argtypes = [_P, _P, C.c_int64, C.c_int]
     lib.orc_count_tiles.restype = C.c_int
@@ -95,6 +98,15 @@ def count_forward_sorted_range(beg, adj, lo: int, hi: int, min_deg: int = 2, thr
                                                C.byref(out))
     assert rc == 0
     return int(out.value)
+
+
+def count_forward_stride(beg, adj, start: int, stride: int, min_deg: int = 2, threads: int = 1):
+    """(count, arcs) over source vertices start, start + stride, ... of a CSR with sorted rows."""
+    out, arcs = C.c_uint64(), C.c_uint64()
+    rc = load().orc_count_forward_stride(_p(beg), _p(adj), beg.size - 1, start, stride, min_deg, threads,
+                                         C.byref(out), C.byref(arcs))
+    assert rc == 0
+    return int(out.value), int(arcs.value)
 
 
 def wedges(beg, adj, min_deg: int = 2) -> int:
@@ -212,6 +224,12 @@ def gen_ba(n: int, d: int, seed: int) -> np.ndarray:
     out = np.zeros((n * d, 2), dtype=np.int32)
     load().orc_gen_ba(n, d, seed, _p(out))
     return out
+
+
+def batch_graph_pairs(kind: str, n: int, param: int, npairs: int, seed: int) -> np.ndarray:
+    """One batch graph's pairs (local ids) from the CPU twin of its generator: Erdos-Renyi with
+    `npairs` uniform pairs, or Barabasi-Albert with `param` edges per vertex."""
+    return gen_er(n, npairs, seed) if kind == "er" else gen_ba(n, param, seed)
 
 
 # ---- the reference kernel rebuilt for sm_103a (GPU host only) ------------------------------------

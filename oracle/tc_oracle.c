@@ -74,6 +74,7 @@ typedef struct {
   const i32 *adj;
   const i32 *sorted; /* per-row sorted copy of adj */
   i64 lo, n;         /* source vertices [lo, n) */
+  i64 stride;        /* every stride-th of them: lo, lo + stride, ... */
   int min_deg;
   atomic_llong next;
   atomic_ullong total;
@@ -102,11 +103,13 @@ static void *count_worker(void *arg) {
   count_job *J = (count_job *)arg;
   const i64 CH = 256;
   u64 local = 0;
+  const i64 samples = (J->n - J->lo + J->stride - 1) / J->stride;
   for (;;) {
-    i64 v0 = J->lo + atomic_fetch_add(&J->next, CH);
-    if (v0 >= J->n) break;
-    i64 v1 = v0 + CH < J->n ? v0 + CH : J->n;
-    for (i64 v = v0; v < v1; ++v) {
+    i64 k0 = atomic_fetch_add(&J->next, CH);
+    if (k0 >= samples) break;
+    i64 k1 = k0 + CH < samples ? k0 + CH : samples;
+    for (i64 k = k0; k < k1; ++k) {
+      const i64 v = J->lo + k * J->stride;
       i64 b = J->beg[v], e = J->beg[v + 1];
       if (e - b < J->min_deg) continue;
       const i32 *rv = J->sorted + b;
@@ -120,10 +123,10 @@ static void *count_worker(void *arg) {
   return NULL;
 }
 
-static void run_count(const i64 *beg, const i32 *adj, const i32 *sorted, i64 lo, i64 hi, int min_deg,
+static void run_count(const i64 *beg, const i32 *adj, const i32 *sorted, i64 lo, i64 hi, i64 stride, int min_deg,
                       int threads, u64 *out) {
   count_job J;
-  J.beg = beg; J.adj = adj; J.sorted = sorted; J.lo = lo; J.n = hi; J.min_deg = min_deg;
+  J.beg = beg; J.adj = adj; J.sorted = sorted; J.lo = lo; J.n = hi; J.stride = stride; J.min_deg = min_deg;
   atomic_init(&J.next, 0);
   atomic_init(&J.total, 0);
   if (threads <= 1) {
@@ -150,7 +153,7 @@ int orc_count_forward(const i64 *beg, const i32 *adj, i64 n, int min_deg, int th
   for (i64 v = 0; v < n; ++v)
     if (beg[v + 1] - beg[v] > 1) qsort(sorted + beg[v], (size_t)(beg[v + 1] - beg[v]), sizeof(i32), cmp_i32);
   *out = 0;
-  run_count(beg, adj, sorted, 0, n, min_deg, threads, out);
+  run_count(beg, adj, sorted, 0, n, 1, min_deg, threads, out);
   free(sorted);
   return 0;
 }
@@ -163,7 +166,24 @@ int orc_count_forward_sorted_range(const i64 *beg, const i32 *adj, i64 n, i64 lo
   if (hi > n) hi = n;
   *out = 0;
   if (lo >= hi) return 0;
-  run_count(beg, adj, adj, lo, hi, min_deg, threads, out);
+  run_count(beg, adj, adj, lo, hi, 1, min_deg, threads, out);
+  return 0;
+}
+
+/* The same quantity over the source vertices start, start + stride, ... < n of a CSR with sorted
+ * rows: a systematic sample of rows of every degree class (the bounded CPU-baseline sample on
+ * graphs whose whole count takes minutes).  *arcs receives the sampled vertices' arc count. */
+int orc_count_forward_stride(const i64 *beg, const i32 *adj, i64 n, i64 start, i64 stride, int min_deg, int threads,
+                             u64 *out, u64 *arcs) {
+  *out = 0;
+  *arcs = 0;
+  if (stride < 1 || start < 0) return -1;
+  if (start >= n) return 0;
+  u64 a = 0;
+  for (i64 v = start; v < n; v += stride)
+    if (beg[v + 1] - beg[v] >= min_deg) a += (u64)(beg[v + 1] - beg[v]);
+  *arcs = a;
+  run_count(beg, adj, adj, start, n, stride, min_deg, threads, out);
   return 0;
 }
 

@@ -29,7 +29,7 @@ def small_batch():
     del pairs
     expect = []
     for s in specs:
-        ob, oa = O.build_csr(B.oracle_graph_pairs(s), s.n)
+        ob, oa = O.build_csr(O.batch_graph_pairs(s.kind, s.n, s.param, s.npairs, s.seed), s.n)
         expect.append(O.count_forward(ob, oa, threads=8))
     return specs, beg, adj, gv, np.array(expect, dtype=np.uint64)
 
@@ -55,7 +55,7 @@ def test_batch_graph_ranges_and_single_calls(small_batch):
     with T.Context() as ctx:
         for g in list(range(0, len(specs), 7)):
             gb, ga = B.graph_csr(beg, adj, gv, g)
-            ob, oa = O.build_csr(B.oracle_graph_pairs(specs[g]), specs[g].n)
+            ob, oa = O.build_csr(O.batch_graph_pairs(specs[g].kind, specs[g].n, specs[g].param, specs[g].npairs, specs[g].seed), specs[g].n)
             assert gb.numel() - 1 == ob.size - 1 and ga.numel() == oa.size  # same vertices and arcs
             if ga.numel():
                 r = T.count_csr(gb, ga, ctx=ctx, schedule=T.SCHED_PLAIN)

@@ -21,7 +21,7 @@ def test_cli_line(tmp_path):
     r = subprocess.run([CLI, str(tmp_path), "1", "1024", "1024", "1"], capture_output=True, text=True, timeout=120)
     assert r.returncode == 0, r.stdout + r.stderr
     line = r.stdout.strip("\n")
-    assert line.endswith(" ")  # "%s,%d,%d,%lld,%f,%f \n" (Without-graph-partition/mpi_main.cpp:124)
+    assert line.endswith(" ")  # "%s,%d,%d,%lld,%f,%f \n" (Without-graph-partition/mpi_main.cpp:115)
     folder, n, m, tri, t, teps = line.strip().split(",")
     assert folder == str(tmp_path)
     assert int(n) == z["ref_beg"].size - 1 and int(m) == z["ref_adj"].size
@@ -59,3 +59,29 @@ def test_python_operator(tmp_path):
     assert a.degree == a.edge_count // a.vertices and a.time > 0
     b = T.Triangle_count(1, str(tmp_path), T.arguments(), 2, 1024, 1024, 1)
     assert b.count == 0 and b.edge_count == a.edge_count
+
+
+def test_reference_style_caller_links(tmp_path):
+    """A main program written against the reference's own TC.cuh declarations (a fixture with the
+    declarations of Without-graph-partition/TC.cuh:1-10) compiles unchanged and links against
+    libtrust_tc.so, the relink recipe of INTEGRATION.md section 1, then counts a golden folder."""
+    fx = os.path.join(ROOT, "tests", "fixtures", "ref_caller")
+    lib_dir = os.path.join(ROOT, "trust_gb300")
+    exe = str(tmp_path / "trianglecounting.bin")
+    obj = str(tmp_path / "main.o")
+    cc = subprocess.run(["g++", "-c", "-I" + fx, os.path.join(fx, "main.cpp"), "-o", obj], capture_output=True,
+                        text=True, timeout=120)
+    assert cc.returncode == 0, cc.stderr
+    ld = subprocess.run(["g++", obj, "-L" + lib_dir, "-ltrust_tc", "-Wl,-rpath," + lib_dir, "-o", exe],
+                        capture_output=True, text=True, timeout=120)
+    assert ld.returncode == 0, ld.stderr
+    z = np.load(os.path.join(GOLD, "rmat_s12.npz"))
+    folder = tmp_path / "graph"
+    folder.mkdir()
+    T.save_folder(str(folder), z["ref_beg"], z["ref_adj"])
+    r = subprocess.run([exe, str(folder), "2", "1024", "1024", "1"], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
+    fields = r.stdout.strip().split(",")
+    assert fields[0] == str(folder)
+    assert int(fields[1]) == z["ref_beg"].size - 1 and int(fields[2]) == z["ref_adj"].size
+    assert int(fields[3]) == int(z["nx_triangles"][0])

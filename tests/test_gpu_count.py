@@ -131,6 +131,10 @@ def test_autotune(ctx):
     assert ms > 0 and cfg["threads"] in (0, 128, 256, 512, 1024) and cfg["chunk"] in (0, 4, 8, 16)
     assert cfg["schedule"] in (T.SCHED_LEARNED, T.SCHED_TUNED, T.SCHED_PLAIN)
     assert T.count_csr(beg, adj, ctx=ctx, **cfg).triangles == expect
+    # a budget spent by the first (base) measurement: no other candidate starts
+    cfg0, ms0 = T.autotune(beg, adj, ctx, repeats=1, time_budget_s=1e-9)
+    assert ms0 > 0 and cfg0 == {"threads": 0, "warp_max": 0, "chunk": 0, "hub_cluster": 0,
+                                "schedule": T.SCHED_LEARNED}
     # a graph with a row above the CTA table: the hub cluster size is tuned too
     import torch
     D = 20_000
@@ -367,3 +371,52 @@ def test_learned_schedule_on_rmat(ctx):
     for schedule in (T.SCHED_LEARNED, T.SCHED_TUNED, T.SCHED_PLAIN):
         for split in (-1, 0, 1):
             assert T.count_csr(beg, adj, ctx=ctx, schedule=schedule, direction_split=split).triangles == expect
+
+
+def test_bounded_wait_runs_out_safely(ctx):
+    """Failure detection without a fault: the hub kernel's copy barrier is armed with no copy
+    issued (opts.test_wait_expiry), so its bounded wait (a few thousand cycles) runs out with
+    nothing in flight.  The call reports TRUST_TC_E_DEVICE, the kernel's plain-load fallback still
+    gives the exact count, and the next normal call on the same context is unaffected."""
+    import ctypes as C
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "k150.npz"))
+    expect = int(z["nx_triangles"][0])
+    db, da = _dev(z["ref_beg"], z["ref_adj"])
+    o = T._opts(ptr_kind=T.DEVICE, warp_max=32, block_max=64)  # rows above 64 entries: hub kernel
+    o.test_wait_expiry = 1
+    r = _lib.Result()
+    rc = T.load().trust_tc_count_csr(ctx.handle, C.c_void_p(db.data_ptr()), C.c_void_p(da.data_ptr()),
+                                     db.numel() - 1, da.numel(), C.byref(o), C.byref(r))
+    assert rc == _lib.E_DEVICE
+    assert r.triangles == expect and r.class_sizes[7] > 0
+    again = T.count_csr(db, da, ctx=ctx, warp_max=32, block_max=64)
+    assert again.triangles == expect
+
+
+def test_row_range_slices(ctx):
+    """Source-row slices (opts.row_begin/row_end) count exactly the oracle's rows and sum to the
+    whole count under every schedule; bad ranges are refused."""
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "rmat_s12.npz"))
+    pairs = T.gen_rmat(14, 16, seed=4)
+    beg, adj = T.build_csr(pairs, 1 << 14)
+    hb, ha = beg.cpu().numpy(), adj.cpu().numpy()
+    n = hb.size - 1
+    cuts = [0, 1, 7, 100, 1000, n // 2, n]
+    for sch, split in ((T.SCHED_LEARNED, -1), (T.SCHED_LEARNED, 1), (T.SCHED_TUNED, 0), (T.SCHED_PLAIN, 0)):
+        total = 0
+        for lo, hi in zip(cuts[:-1], cuts[1:]):
+            r = T.count_csr(beg, adj, ctx=ctx, schedule=sch, direction_split=split, row_range=(lo, hi))
+            assert r.triangles == O.count_forward_sorted_range(hb, ha, lo, hi, 2, 4), (sch, split, lo, hi)
+            total += r.triangles
+        assert total == T.count_csr(beg, adj, ctx=ctx, schedule=sch).triangles
+    # host input and an empty range
+    assert T.count_csr(hb, ha, ctx=ctx, row_range=(5, 5)).triangles == 0
+    # a range on the unsorted golden rows (no split possible) with forced hub rows
+    zb, za = _dev(z["ref_beg"], z["ref_adj"])
+    m = z["ref_beg"].size - 1
+    r = T.count_csr(zb, za, ctx=ctx, warp_max=32, block_max=64, row_range=(0, m // 3))
+    assert r.triangles == O.count_forward_sorted_range(z["ref_beg"], np.concatenate(
+        [np.sort(z["ref_adj"][z["ref_beg"][v]:z["ref_beg"][v + 1]]) for v in range(m)]).astype(np.int32), 0, m // 3, 2, 1)
+    for bad in ((-1, 5), (6, 5), (0, n + 1)):
+        with pytest.raises(T.TrustTcError):
+            T.count_csr(beg, adj, ctx=ctx, row_range=bad)

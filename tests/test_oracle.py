@@ -170,3 +170,18 @@ def test_batch_specs_stream():
     assert ns.min() >= 50 and ns.max() <= 50_000
     assert sum(x.kind == "er" for x in s) == 2048
     assert all(4 <= x.param <= 64 for x in s if x.kind == "er") and all(2 <= x.param <= 16 for x in s if x.kind == "ba")
+
+
+def test_strided_sample_counter():
+    """The systematic row sample used by the bench's CPU baseline: the strided counts over every
+    offset partition the rows, so they sum to the whole count, and the arcs they report too."""
+    z = _golden("chung_lu_3000")
+    beg = z["ref_beg"]
+    adj = np.concatenate([np.sort(z["ref_adj"][beg[v]:beg[v + 1]]) for v in range(beg.size - 1)]).astype(np.int32)
+    whole = O.count_forward_sorted_range(beg, adj, 0, beg.size - 1, 2, 1)
+    assert whole == int(z["nx_triangles"][0])
+    for stride in (1, 3, 7):
+        parts = [O.count_forward_stride(beg, adj, s, stride, 2, 4) for s in range(stride)]
+        assert sum(c for c, _ in parts) == whole
+        d = np.diff(beg)
+        assert sum(a for _, a in parts) == int(d[d >= 2].sum())

@@ -78,6 +78,13 @@ def test_noalloc_rejects_what_it_cannot_hold():
     rc = T.load().trust_tc_count_csr_noalloc(b.ctypes.data_as(C.c_void_p), a.ctypes.data_as(C.c_void_p),
                                               b.size - 1, a.size, C.byref(o), C.byref(r))
     assert rc == _lib.E_UNSUPPORTED
+    # per-vertex cycle recording and source-row ranges belong to the regular entry point only
+    for field in ("record_cycles", "row_end"):
+        o = T._opts(ptr_kind=T.DEVICE)
+        setattr(o, field, 1)
+        rc = T.load().trust_tc_count_csr_noalloc(C.c_void_p(beg.data_ptr()), C.c_void_p(adj.data_ptr()),
+                                                  beg.numel() - 1, adj.numel(), C.byref(o), C.byref(r))
+        assert rc == _lib.E_UNSUPPORTED, field
     # and it still counts correctly afterwards
     rc, r = _noalloc(beg, adj)
     assert rc == _lib.OK and r.triangles == int(z["nx_triangles"][0])

@@ -113,10 +113,13 @@ def _is_torch_cuda(x) -> bool:
 
 def count_csr(beg, adj, *, ctx: Context | None = None, threads=0, blocks=0, chunk=0, stream=None,
               validate=VALIDATE_FULL, warp_max=0, block_max=0, schedule=SCHED_LEARNED,
-              cycles=None, direction_split=-1, model=None, hub_cluster=0) -> CountResult:
+              cycles=None, direction_split=-1, model=None, hub_cluster=0,
+              row_range: tuple[int, int] | None = None) -> CountResult:
     """Count over a CSR held in numpy arrays (host) or contiguous torch CUDA tensors (device).
 
-    `stream` is a cudaStream_t value (e.g. torch.cuda.current_stream().cuda_stream)."""
+    `stream` is a cudaStream_t value (e.g. torch.cuda.current_stream().cuda_stream).
+    `row_range` = (lo, hi): count only the arcs whose source row lies in [lo, hi); the whole graph
+    is still validated and probed, so the slices of a graph sum to its count."""
     lib = load()
     if _is_torch_cuda(beg):
         import torch
@@ -133,6 +136,11 @@ def count_csr(beg, adj, *, ctx: Context | None = None, threads=0, blocks=0, chun
     o = _opts(threads, blocks, chunk, kind, validate, warp_max, block_max, stream, schedule=schedule)
     o.direction_split = direction_split
     o.hub_cluster = hub_cluster
+    if row_range is not None:
+        lo, hi = int(row_range[0]), int(row_range[1])
+        if hi <= 0:  # the C field's 0 means "all rows"; an explicit range ends at a positive row
+            raise ValueError("row_range end must be positive")
+        o.row_begin, o.row_end = lo, hi
     if model is not None:  # host float32 array of model_floats() entries (learned schedule)
         model = np.ascontiguousarray(model, dtype=np.float32)
         o.model = model.ctypes.data_as(C.c_void_p)
@@ -174,14 +182,17 @@ def count_partitioned(folder: str, parts: int, threads=0, blocks=0, chunk=0, sch
     return _result(r)
 
 
-def autotune(beg, adj, ctx: Context, repeats: int = 3, schedule=SCHED_LEARNED) -> tuple[dict, float]:
+def autotune(beg, adj, ctx: Context, repeats: int = 3, schedule=SCHED_LEARNED,
+             time_budget_s: float = 0.0) -> tuple[dict, float]:
     """Fastest launch parameters for this device CSR (torch CUDA tensors): (count_csr keyword
-    arguments, median call ms)."""
+    arguments, median call ms).  `time_budget_s` > 0 stops starting new candidates once the calls
+    made add up to that much time."""
     o = _opts(ptr_kind=DEVICE, schedule=schedule)
     best = _lib.Opts()
     ms = C.c_double()
     check(load().trust_tc_autotune(ctx.handle, C.c_void_p(beg.data_ptr()), C.c_void_p(adj.data_ptr()), beg.numel() - 1,
-                                   adj.numel(), C.byref(o), repeats, C.byref(best), C.byref(ms)), "trust_tc_autotune")
+                                   adj.numel(), C.byref(o), repeats, float(time_budget_s), C.byref(best),
+                                   C.byref(ms)), "trust_tc_autotune")
     return ({"threads": best.threads_per_block, "warp_max": best.warp_max_degree, "chunk": best.chunk,
              "hub_cluster": best.hub_cluster, "schedule": best.schedule}, ms.value)
 
@@ -204,7 +215,7 @@ def count_tiles(beg, adj, parts: int, budget_bytes: int = 0, threads=0, blocks=0
 def Triangle_count(rank: int, name: str, args: arguments, total_process: int, n_threads: int, n_blocks: int,
                    chunk_size: int, partition_num: int | None = None) -> arguments:  # noqa: N802
     """The reference operator.  One GPU: rank 0 returns the whole count, other ranks 0, so the
-    caller's SUM over ranks (Without-graph-partition/mpi_main.cpp:119) is unchanged.  Where the
+    caller's SUM over ranks (Without-graph-partition/mpi_main.cpp:110-112) is unchanged.  Where the
     reference prints and exits on error, this raises TrustTcError."""
     del total_process
     if rank > 0:

@@ -34,6 +34,9 @@ class Opts(C.Structure):
         ("model", C.c_void_p),
         ("direction_split", C.c_int),
         ("hub_cluster", C.c_int),
+        ("row_begin", C.c_int64),
+        ("row_end", C.c_int64),
+        ("test_wait_expiry", C.c_int),
     ]
 
 
@@ -83,8 +86,8 @@ SIGNATURES = {
     "trust_tc_free_host": (None, [_P]),
     "trust_tc_count_folder": (C.c_int, [C.c_char_p, C.POINTER(Opts), C.POINTER(Result)]),
     "trust_tc_count_partitioned": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(Opts), C.POINTER(Result)]),
-    "trust_tc_autotune": (C.c_int, [_P, _P, _P, C.c_int64, C.c_int64, C.POINTER(Opts), C.c_int, C.POINTER(Opts),
-                                    C.POINTER(C.c_double)]),
+    "trust_tc_autotune": (C.c_int, [_P, _P, _P, C.c_int64, C.c_int64, C.POINTER(Opts), C.c_int, C.c_double,
+                                    C.POINTER(Opts), C.POINTER(C.c_double)]),
     "trust_tc_count_tiles_device": (C.c_int, [_P, _P, C.c_int64, C.c_int64, C.c_int, C.c_size_t, C.POINTER(Opts),
                                               C.POINTER(Result)]),
     "trust_tc_partition_folder": (C.c_int, [C.c_char_p, _P, _P, C.c_int64, C.c_int64, C.c_int]),

@@ -77,12 +77,6 @@ def gen_batch_pairs(specs: list[GraphSpec]):
     return pairs, vbeg
 
 
-def oracle_graph_pairs(spec: GraphSpec) -> np.ndarray:
-    """The same graph's pairs from the CPU oracle (local ids)."""
-    from oracle import oracle as O
-    return O.gen_er(spec.n, spec.npairs, spec.seed) if spec.kind == "er" else O.gen_ba(spec.n, spec.param, spec.seed)
-
-
 def build_batch(pairs, graph_vbeg: np.ndarray):
     """GPU preprocessing of a batch: (beg int64, adj int32, graph_vbeg of the result)."""
     import torch

@@ -6,7 +6,7 @@ Outputs (all git-ignored):
   trust_gb300/trust_tc         the CLI with the reference's argv and output line
   oracle/_build/liboracle.so   CPU oracle (tests, smoke and the bench CPU legs only)
   oracle/_build/liboracle_cuda.so  oracle + the harness that runs the reference kernel cubin
-  oracle/_ref/*                the reference's own code, only where its sources are present
+  oracle/_ref/*                the reference's own code, only where TRUST_REFERENCE_ROOT names its sources
 
 Compiles in parallel and skips outputs newer than their sources.
 """
@@ -118,9 +118,11 @@ def build_oracle() -> None:
         _run(["gcc", "-O2", "-std=c11", "-ffp-contract=off", "-fPIC", "-shared", "-I" + os.path.join(cuda, "include"),
               "-o", ORACLE_CUDA_LIB, drv, src, "-L" + os.path.join(cuda, "lib64", "stubs"), "-lcuda",
               "-lpthread", "-lm"])
-    ref_root = os.environ.get("TRUST_REFERENCE_ROOT", "/root/reference")
+    # the reference's own sources, where the caller names them (TRUST_REFERENCE_ROOT); without it
+    # the reference oracles are used only if an earlier build left them in oracle/_ref/
+    ref_root = os.environ.get("TRUST_REFERENCE_ROOT")
     ref_out = os.path.join(ORACLE, "_ref", "tc_ref_w.cubin")
-    if os.path.isdir(os.path.join(ref_root, "Preprocess")) and not os.path.exists(ref_out):
+    if ref_root and os.path.isdir(os.path.join(ref_root, "Preprocess")) and not os.path.exists(ref_out):
         _run(["sh", os.path.join(ORACLE, "build_ref.sh"), ref_root])
 
 

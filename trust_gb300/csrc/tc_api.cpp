@@ -222,6 +222,8 @@ int count_device(trust_tc_ctx *c, const DevGraph3 &g, const trust_tc_opts &o, bo
   int rc = resolve_cfg(c, o, same, &cfg);
   if (rc) return rc;
   TcControl *ctl = c->d_ctl;
+  // source rows whose arcs are counted (one CSR): [row_lo, row_hi); row_hi = -1 means all rows
+  const int64_t row_lo = g.row_lo, row_hi = g.row_hi > 0 ? g.row_hi : -1;
   TC_CUDA_TRY(cudaEventRecord(c->ev[0], st));
   TC_CUDA_TRY(cudaMemsetAsync(ctl, 0, sizeof(TcControl), st));
   ListOffsets off{};
@@ -233,7 +235,7 @@ int count_device(trust_tc_ctx *c, const DevGraph3 &g, const trust_tc_opts &o, bo
     if (rc) return rc;
     TC_CUDA_TRY(cudaEventRecord(c->ev[1], st));
     rc = launch_check_classify(g.begA, g.adjA, g.rows, g.mA, check_ids, g.min_deg, cfg.warp_max, cfg.cta_max,
-                               o.schedule, ctl, c->d_lists, c->num_sms, st);
+                               o.schedule, ctl, c->d_lists, c->num_sms, st, row_lo, row_hi);
     if (rc) return rc;
   } else {
     // 1. validation of every distinct CSR: offsets always, ids on request
@@ -251,7 +253,7 @@ int count_device(trust_tc_ctx *c, const DevGraph3 &g, const trust_tc_opts &o, bo
     // 2. classification histogram
     TC_CUDA_TRY(cudaEventRecord(c->ev[1], st));
     rc = launch_classify(0, g.begA, g.begB, g.rows, g.min_deg, cfg.warp_max, cfg.cta_max, ctl, c->d_lists,
-                         off, c->num_sms, st, o.schedule, g.rowmap);
+                         off, c->num_sms, st, o.schedule, g.rowmap, nullptr, row_lo, row_hi);
     if (rc) return rc;
   }
   TC_CUDA_TRY(cudaMemcpyAsync(c->h_ctl, ctl, sizeof(TcControl), cudaMemcpyDeviceToHost, st));
@@ -283,14 +285,14 @@ int count_device(trust_tc_ctx *c, const DevGraph3 &g, const trust_tc_opts &o, bo
     // (the pass also checks that rows are duplicate-free, which the split needs); with a model,
     // the class histogram under its decisions follows on the stream before the one readback
     rc = split_plan(c, g.begA, g.adjA, g.rows, g.mA, st, d_model, cfg.warp_max, cfg.cta_max, TC_PROMOTE_LOG2,
-                    cfg.threads / 32, ctl);
+                    cfg.threads / 32, ctl, row_lo, row_hi);
     if (rc) return rc;
     if (d_model) {
       dec = c->d_dec;
       pred = c->d_pred;
       TC_CUDA_TRY(cudaMemsetAsync(ctl->class_count, 0, sizeof ctl->class_count, st));
       rc = launch_classify(0, g.begA, g.begB, g.rows, g.min_deg, cfg.warp_max, cfg.cta_max, ctl, c->d_lists, off,
-                           c->num_sms, st, o.schedule, g.rowmap, dec);
+                           c->num_sms, st, o.schedule, g.rowmap, dec, row_lo, row_hi);
       if (rc) return rc;
     }
     TC_CUDA_TRY(cudaMemcpyAsync(c->h_ctl, ctl, sizeof(TcControl), cudaMemcpyDeviceToHost, st));
@@ -397,7 +399,7 @@ int count_device(trust_tc_ctx *c, const DevGraph3 &g, const trust_tc_opts &o, bo
   // 3. scatter the class lists
   if (!lists_done) {
     rc = launch_classify(1, g.begA, g.begB, g.rows, g.min_deg, cfg.warp_max, cfg.cta_max, ctl, c->d_lists,
-                         off, c->num_sms, st, o.schedule, g.rowmap, dec);
+                         off, c->num_sms, st, o.schedule, g.rowmap, dec, row_lo, row_hi);
     if (rc) return rc;
   }
   if (pred) {  // heaviest first inside the huge, CTA and warp queues
@@ -416,6 +418,7 @@ int count_device(trust_tc_ctx *c, const DevGraph3 &g, const trust_tc_opts &o, bo
   a.chunk = cfg.chunk;
   a.split = split;
   a.rowmap = g.rowmap;
+  a.test_wait_expiry = o.test_wait_expiry;
   if (h.class_count[TC_CLASS_CTA] > 0) {
     // long-row lists: one per CTA, as long as the largest CTA-class row
     const int cap = (int)std::min<int64_t>(h.max_out_degree, cfg.cta_max);
@@ -439,6 +442,7 @@ int count_device(trust_tc_ctx *c, const DevGraph3 &g, const trust_tc_opts &o, bo
   trust_tc_result rb;
   memset(&rb, 0, sizeof rb);
   float t_build = 0;
+  int rb_status = 0;  // TC_DEV_* bits of the second pass
   if (split) {
     // Second pass: arcs (v,u) with d(u) > d(v), hashed on u's row, streaming the sources' rows (a
     // tile job: tables from C's rows, probe rows from A's).  It runs on the context's second stream
@@ -447,6 +451,10 @@ int count_device(trust_tc_ctx *c, const DevGraph3 &g, const trust_tc_opts &o, bo
     // first pass reads.  Its in-list build and setup (host round trips included) hide under the
     // first pass, and its CTAs take SMs as the first pass's tail drains.
     rc = split_second_pass(c, g, o, same, h.max_out_degree, &rb, &t_build);
+    if (rc == TRUST_TC_E_DEVICE) {  // its result is filled; reported with the first pass's below
+      rb_status = TC_DEV_WAIT_LIMIT;
+      rc = TRUST_TC_OK;
+    }
     if (rc) {
       cudaStreamSynchronize(st);
       return rc;
@@ -456,7 +464,6 @@ int count_device(trust_tc_ctx *c, const DevGraph3 &g, const trust_tc_opts &o, bo
   TC_CUDA_TRY(cudaEventRecord(c->ev[4], st));
   TC_CUDA_TRY(cudaStreamSynchronize(st));
   const TcControl done = *c->h_ctl;
-  if (done.status & (TC_DEV_TABLE_FULL | TC_DEV_WAIT_LIMIT)) return TRUST_TC_E_DEVICE;
   float t_kernel = 0, t_count = 0, t_call = 0;
   TC_CUDA_TRY(cudaEventElapsedTime(&t_kernel, c->ev[1], c->ev[3]));
   TC_CUDA_TRY(cudaEventElapsedTime(&t_count, c->ev[2], c->ev[3]));
@@ -475,6 +482,9 @@ int count_device(trust_tc_ctx *c, const DevGraph3 &g, const trust_tc_opts &o, bo
   for (int k = 0; k < TC_NUM_CLASSES; ++k) r->class_sizes[k] = h.class_count[k];
   r->direction_split = split;
   r->split_saving_ms = saving_ms;
+  // a bounded wait that ran out (the kernel fell back to plain loads: the count above is exact) or
+  // a full table (never expected: tables hold twice their row) is reported after the result
+  if ((done.status | rb_status) & (TC_DEV_TABLE_FULL | TC_DEV_WAIT_LIMIT)) return TRUST_TC_E_DEVICE;
   return TRUST_TC_OK;
 }
 
@@ -516,6 +526,7 @@ static int split_second_pass(trust_tc_ctx *c, const DevGraph3 &g, const trust_tc
     gb.rows = sr.rows;
     gb.min_deg = 1;
     gb.split_ok = 0;
+    gb.row_lo = gb.row_hi = 0;  // work rows are in-list chunks: the range was applied when planning
     gb.max_deg_A = max_out_degree;  // tables are whole rows (of the graph, or of C), not in-list chunks
     trust_tc_opts ob = o;
     ob.schedule = TRUST_TC_SCHED_TUNED;
@@ -615,8 +626,9 @@ int trust_tc_validate_csr(const int64_t *beg, const int32_t *adj, int64_t n, int
 }
 
 int trust_tc_autotune(trust_tc_ctx *ctx, const int64_t *beg, const int32_t *adj, int64_t n, int64_t m,
-                      const trust_tc_opts *base, int repeats, trust_tc_opts *best, double *best_ms) {
-  if (!ctx || !best || repeats < 1) return TRUST_TC_E_ARG;
+                      const trust_tc_opts *base, int repeats, double time_budget_s, trust_tc_opts *best,
+                      double *best_ms) {
+  if (!ctx || !best || repeats < 1 || time_budget_s < 0) return TRUST_TC_E_ARG;
   trust_tc_opts o;
   if (base) o = *base; else trust_tc_opts_init(&o);
   if (o.ptr_kind != TRUST_TC_DEVICE || o.record_cycles) return TRUST_TC_E_ARG;
@@ -641,19 +653,25 @@ int trust_tc_autotune(trust_tc_ctx *ctx, const int64_t *beg, const int32_t *adj,
     *ms = v[v.size() / 2];
     return TRUST_TC_OK;
   };
+  // device time spent on candidates so far; once past the budget no new candidate starts
+  double spent_ms = 0;
+  const double budget_ms = time_budget_s * 1e3;
   double cur = 0;
   int rc = time_of(o, &cur);
   if (rc) return rc;
+  spent_ms += cur * repeats;
   // coordinate descent over the launch parameters, each from the best so far
   auto sweep = [&](int trust_tc_opts::*field, std::initializer_list<int> values) -> int {
     for (int val : values) {
       if (o.*field == val) continue;
+      if (budget_ms > 0 && spent_ms >= budget_ms) break;
       trust_tc_opts t = o;
       t.*field = val;
       double ms = 0;
       int e = time_of(t, &ms);
       if (e == TRUST_TC_E_ARG) continue;  // not a valid combination (e.g. CTA bound below the warp bound)
       if (e) return e;
+      spent_ms += ms * repeats;
       if (ms < cur) {
         cur = ms;
         o = t;
@@ -683,6 +701,9 @@ int trust_tc_count_csr(trust_tc_ctx *ctx, const int64_t *beg, const int32_t *adj
   if (o.schedule != TRUST_TC_SCHED_PLAIN && o.schedule != TRUST_TC_SCHED_LEARNED && o.schedule != TRUST_TC_SCHED_TUNED)
     return TRUST_TC_E_ARG;
   if (n >= ((int64_t)1 << 31) || m >= ((int64_t)1 << 31)) return TRUST_TC_E_TOO_LARGE;
+  if (o.row_begin < 0 || o.row_end < 0 || o.row_end > n || (o.row_end > 0 && o.row_begin > o.row_end) ||
+      (o.row_end == 0 && o.row_begin > n))
+    return TRUST_TC_E_ARG;
   uint64_t *cycles = r->vertex_cycles;
   memset(r, 0, sizeof *r);
   r->vertex_cycles = cycles;
@@ -731,6 +752,8 @@ int trust_tc_count_csr(trust_tc_ctx *ctx, const int64_t *beg, const int32_t *adj
     g.mA = g.mB = g.mC = m;
     g.boundA = g.boundB = g.boundC = n;
     g.min_deg = 2;
+    g.row_lo = o.row_begin;
+    g.row_hi = o.row_end > 0 ? o.row_end : n;
     rc = count_device(c, g, o, check_ids, r);
   }
   if (slot) {  // count_device has synchronised (or failed): the slot is free for the next stage

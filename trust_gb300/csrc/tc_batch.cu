@@ -1,6 +1,6 @@
 // tc_batch.cu — many graphs counted by one CUDA-graph launch.
 //
-// The reference counts one graph per run (Without-graph-partition/mpi_main.cpp:90-124): a batch
+// The reference counts one graph per run (Without-graph-partition/mpi_main.cpp:75-119): a batch
 // of thousands of small graphs through it is a loop of runs, each paying its own launches and
 // host synchronisations.  Here a batch is the disjoint union of its graphs in one oriented CSR
 // (trust_tc_build_batch_device keeps every graph a contiguous row range), and one captured CUDA

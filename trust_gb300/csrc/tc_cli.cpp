@@ -1,11 +1,11 @@
 // tc_cli.cpp — command-line program with the reference's argv and output line.
 //
-//   trust_tc <folder> <nGPUs> <threads> <blocks> <chunk>          (Without-graph-partition/mpi_main.cpp:84-128)
+//   trust_tc <folder> <nGPUs> <threads> <blocks> <chunk>          (Without-graph-partition/mpi_main.cpp:75-119)
 //   trust_tc <folder> <nGPUs> <threads> <blocks> <chunk> <n>      (With-graph-partition/mpi_main.cpp:75-127)
 //
 // Logical ranks are looped as the reference does when fewer processes than ranks run
-// (mpi_main.cpp:104-113); on one GPU rank 0 carries the whole count.  Output, unchanged:
-//   "%s,%d,%d,%lld,%f,%f \n"  folder, vertices, edges, triangles, max time, GTEPS   (W main :124)
+// (Without-graph-partition/mpi_main.cpp:94-104); on one GPU rank 0 carries the whole count.  Output, unchanged:
+//   "%s,%d,%d,%lld,%f,%f \n"  folder, vertices, edges, triangles, max time, GTEPS   (W main :115)
 //   "\n%s,triangle:%lld,%f,%f\n" folder, triangles, min time, max time            (P main :123)
 #include <stdio.h>
 #include <stdlib.h>

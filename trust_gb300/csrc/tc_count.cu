@@ -337,11 +337,13 @@ __device__ __forceinline__ int classify(int dA, int dB, int min_deg, int warp_ma
 }
 
 // pass 0: histogram of classes.  pass 1: scatter vertex ids into per-class lists.
+// Rows outside [row_lo, row_hi) are classed as skipped (their arcs are not counted).
 template <int PASS>
 __global__ void class_kernel(const int64_t *__restrict__ begA, const int64_t *__restrict__ begB,
                              int64_t rows, int min_deg, int warp_max, int cta_max, int plain,
                              const int *__restrict__ rowmap, const unsigned char *__restrict__ dec,
-                             TcControl *ctl, int *__restrict__ lists, ListOffsets off) {
+                             TcControl *ctl, int *__restrict__ lists, ListOffsets off, int64_t row_lo,
+                             int64_t row_hi) {
   __shared__ int s_hist[TC_NUM_CLASSES];
   __shared__ int s_base[TC_NUM_CLASSES];
   const int lane = threadIdx.x & 31;
@@ -357,6 +359,7 @@ __global__ void class_kernel(const int64_t *__restrict__ begA, const int64_t *__
       int dB = (begB == begA && !rowmap) ? dA : (int)(tc_ld_nc(begB + v + 1) - tc_ld_nc(begB + v));
       c = classify(dA, dB, min_deg, warp_max, cta_max, plain);
       if (dec && dA == dB && dA > 32) c = dec[v];  // the learned schedule's decision for long rows
+      if (v < row_lo || v >= row_hi) c = TC_CLASS_SKIP;
     }
     // warp-aggregated block histogram, then one global reservation per class per block
     unsigned peers = __match_any_sync(TC_FULL_MASK, c);
@@ -386,14 +389,17 @@ __global__ void class_kernel(const int64_t *__restrict__ begA, const int64_t *__
 // rows, TC_CC_PER of them per thread with all their offsets loaded up front: it counts its
 // classes in shared memory, reserves its share of every class list with one global atomic per
 // class, and scatters from the classes kept in registers.  Rows with bad offsets are flagged and
-// left out of every list.  The id check is a separate grid-strided stream over adj.
+// left out of every list.  The id check is a separate grid-strided stream over adj.  Rows outside
+// [row_lo, row_hi) are validated and measured (maximum out-degree, arcs in long rows) but listed
+// in no class: their arcs are not counted.
 constexpr int TC_CC_THREADS = 256;
 constexpr int TC_CC_PER = 8;
 constexpr int TC_CC_ROWS = TC_CC_THREADS * TC_CC_PER;
 
 __global__ void __launch_bounds__(TC_CC_THREADS) check_class_kernel(
     const int64_t *__restrict__ beg, const int32_t *__restrict__ adj, int64_t rows, int64_t m, int check_ids,
-    int min_deg, int warp_max, int cta_max, int plain, TcControl *ctl, int *__restrict__ lists) {
+    int min_deg, int warp_max, int cta_max, int plain, TcControl *ctl, int *__restrict__ lists, int64_t row_lo,
+    int64_t row_hi) {
   __shared__ int s_hist[TC_NUM_CLASSES];
   __shared__ int s_base[TC_NUM_CLASSES];
   const unsigned lt = tc_lanemask_lt();
@@ -422,7 +428,7 @@ __global__ void __launch_bounds__(TC_CC_THREADS) check_class_kernel(
         const int d = (int)(hi[k] - lo[k]);
         dmax = max(dmax, d);
         if (d > TC_LONG_ROW) long_arcs += (unsigned)d;
-        c = classify(d, d, min_deg, warp_max, cta_max, plain);
+        c = (v >= row_lo && v < row_hi) ? classify(d, d, min_deg, warp_max, cta_max, plain) : TC_CLASS_SKIP;
       }
     }
     cls[k] = c;
@@ -976,21 +982,31 @@ __device__ __forceinline__ void mbar_init(unsigned long long *bar) {
   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
 
+// One thread: arm the barrier for `bytes` of transfers (the phase completes once they arrive).
+__device__ __forceinline__ void mbar_arm(unsigned long long *bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
 // One thread: arm the barrier for `bytes` and start the copy of [src, src + bytes) to dst.
 // src and dst 16-byte aligned, bytes a multiple of 16 (< 2^20).
 // The fence orders this CTA's earlier generic-proxy reads of dst before the copy's writes.
 __device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, unsigned bytes, unsigned long long *bar) {
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+  mbar_arm(bar, bytes);
   asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
                    smem_u32(dst)),
                "l"(src), "r"(bytes), "r"(smem_u32(bar))
                : "memory");
 }
 
-// Wait for the barrier's phase `parity` to complete, giving up after about a second of clock64
-// cycles (returns false then; the caller records TC_DEV_WAIT_LIMIT and stops using the copies).
-__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned parity) {
+// Bounds of the copy waits, in clock64 cycles: about a second at the GB300 clock, and a few
+// thousand for the failure-detection test (whose barrier nothing completes).
+constexpr long long TC_WAIT_CYCLES = 2ll << 30;
+constexpr long long TC_TEST_WAIT_CYCLES = 4096;
+
+// Wait for the barrier's phase `parity` to complete, giving up after `limit` clock64 cycles
+// (returns false then; the caller records TC_DEV_WAIT_LIMIT and stops using the copies).
+__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned parity, long long limit) {
   const long long t0 = clock64();
   for (;;) {
     unsigned done = 0;
@@ -1000,7 +1016,7 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned pari
         : "r"(smem_u32(bar)), "r"(parity)
         : "memory");
     if (done) return true;
-    if (clock64() - t0 > (2ll << 30)) return false;
+    if (clock64() - t0 > limit) return false;
   }
 }
 
@@ -1011,16 +1027,23 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned pari
 // Each CTA stages its contiguous share of the hub row with one TMA bulk copy (the 16-byte aligned
 // interior; the ragged ends, at most 3 entries each, by plain loads) and inserts from shared
 // memory.  Dynamic shared memory: the table share (2^share_log2_max ints) then the staging buffer.
+// A copy whose bounded wait runs out may still be in flight into the staging buffer: the CTA
+// reports TC_DEV_WAIT_LIMIT, reads that share with plain loads, never touches the staging buffer
+// again, and before it exits waits once more (bounded) for the abandoned copy, so its shared
+// memory is not released under a write still landing.  With p.test_wait_expiry the barrier is
+// armed without a copy, so the wait runs out with nothing in flight.
 template <bool SAME>
 __global__ void __launch_bounds__(512, 1) hub_kernel(CountArgs p, int log2C, int share_log2_max) {
   extern __shared__ __align__(16) int smem[];
   __shared__ int next_batch;
   __shared__ __align__(8) unsigned long long bar;
   __shared__ int tma_ok;
+  __shared__ int abandoned;  // 1 + parity of a barrier phase whose copy this CTA stopped waiting for
   int *stage = smem + (1 << share_log2_max);
   if (threadIdx.x == 0) {
     mbar_init(&bar);
     tma_ok = ((reinterpret_cast<uintptr_t>(p.adjA) & 15) == 0);  // 16-byte aligned base: copy the interior
+    abandoned = 0;
   }
   __syncthreads();
   unsigned parity = 0;
@@ -1054,10 +1077,14 @@ __global__ void __launch_bounds__(512, 1) hub_kernel(CountArgs p, int log2C, int
       const long long a0 = (long long)bA + lo, a1 = (long long)bA + hi;
       const long long i0 = (a0 + 3) & ~3ll, i1 = a1 & ~3ll;  // aligned interior [i0, i1)
       if (tma_ok && i1 > i0) {
-        if (threadIdx.x == 0) bulk_copy_g2s(stage, p.adjA + i0, (unsigned)(i1 - i0) * 4u, &bar);
+        const bool copy = !p.test_wait_expiry;
+        if (threadIdx.x == 0) {
+          if (copy) bulk_copy_g2s(stage, p.adjA + i0, (unsigned)(i1 - i0) * 4u, &bar);
+          else mbar_arm(&bar, (unsigned)(i1 - i0) * 4u);  // nothing will arrive
+        }
         for (long long i = a0 + threadIdx.x; i < i0; i += blockDim.x) ok &= set.insert(tc_ld_nc(p.adjA + i));
         for (long long i = i1 + threadIdx.x; i < a1; i += blockDim.x) ok &= set.insert(tc_ld_nc(p.adjA + i));
-        const bool arrived = mbar_wait(&bar, parity);
+        const bool arrived = mbar_wait(&bar, parity, copy ? TC_WAIT_CYCLES : TC_TEST_WAIT_CYCLES);
         parity ^= 1u;
         if (arrived) {
           for (int i = threadIdx.x; i < (int)(i1 - i0); i += blockDim.x) ok &= set.insert(stage[i]);
@@ -1066,7 +1093,10 @@ __global__ void __launch_bounds__(512, 1) hub_kernel(CountArgs p, int log2C, int
           for (long long i = i0 + threadIdx.x; i < i1; i += blockDim.x) ok &= set.insert(tc_ld_nc(p.adjA + i));
         }
         __syncthreads();  // the staging buffer is free again, and every thread saw the same outcome
-        if (threadIdx.x == 0 && !arrived) tma_ok = 0;
+        if (threadIdx.x == 0 && !arrived) {
+          tma_ok = 0;  // no more copies (every thread sees it after the barrier below)
+          if (copy) abandoned = 1 + (int)(parity ^ 1u);
+        }
         __syncthreads();
       } else {
         for (long long i = a0 + threadIdx.x; i < a1; i += blockDim.x) ok &= set.insert(tc_ld_nc(p.adjA + i));
@@ -1089,6 +1119,8 @@ __global__ void __launch_bounds__(512, 1) hub_kernel(CountArgs p, int log2C, int
     cl.sync();  // every probe of this hub is done before any share is cleared again
     if (p.cycles && rank == 0 && threadIdx.x == 0) p.cycles[v] = (unsigned long long)(clock64() - t_start);
   }
+  if (abandoned && threadIdx.x == 0 && !mbar_wait(&bar, (unsigned)(abandoned - 1), TC_WAIT_CYCLES))
+    atomicOr(&p.ctl->status, TC_DEV_WAIT_LIMIT);  // already set when it was abandoned; nothing else to do
   cl.sync();  // no CTA leaves while another may still read its shared memory
 #pragma unroll
   for (int off = 16; off >= 1; off >>= 1) {
@@ -1175,13 +1207,14 @@ int launch_check(const int64_t *beg, const int32_t *adj, int64_t rows, int64_t m
 
 int launch_check_classify(const int64_t *beg, const int32_t *adj, int64_t rows, int64_t m, int check_ids,
                           int min_deg, int warp_max, int cta_max, int schedule, TcControl *ctl, int *lists,
-                          int num_sms, cudaStream_t st) {
+                          int num_sms, cudaStream_t st, int64_t row_lo, int64_t row_hi) {
   // one block per TC_CC_ROWS rows; blocks past the last row only check ids (few rows, many arcs)
   int64_t blocks = std::max<int64_t>(1, (rows + TC_CC_ROWS - 1) / TC_CC_ROWS);
   if (check_ids) blocks = std::max<int64_t>(blocks, std::min<int64_t>((m + 4095) / 4096, (int64_t)num_sms * 8));
   if (blocks > 0x7fffffff) return TRUST_TC_E_TOO_LARGE;
   check_class_kernel<<<(unsigned)blocks, TC_CC_THREADS, 0, st>>>(beg, adj, rows, m, check_ids, min_deg, warp_max,
-                                                                 cta_max, schedule == TRUST_TC_SCHED_PLAIN, ctl, lists);
+                                                                 cta_max, schedule == TRUST_TC_SCHED_PLAIN, ctl, lists,
+                                                                 row_lo, row_hi < 0 ? rows : row_hi);
   TC_NOTE_LAUNCH();
   TC_CUDA_TRY(cudaGetLastError());
   return TRUST_TC_OK;
@@ -1189,16 +1222,18 @@ int launch_check_classify(const int64_t *beg, const int32_t *adj, int64_t rows, 
 
 int launch_classify(int pass, const int64_t *begA, const int64_t *begB, int64_t rows, int min_deg,
                     int warp_max, int cta_max, TcControl *ctl, int *lists, const ListOffsets &off,
-                    int num_sms, cudaStream_t st, int schedule, const int *rowmap, const unsigned char *dec) {
+                    int num_sms, cudaStream_t st, int schedule, const int *rowmap, const unsigned char *dec,
+                    int64_t row_lo, int64_t row_hi) {
   int blocks = (int)std::min<int64_t>((rows + 255) / 256, (int64_t)num_sms * 8);
   blocks = std::max(blocks, 1);
   const int plain = schedule == TRUST_TC_SCHED_PLAIN;
+  if (row_hi < 0) row_hi = rows;
   if (pass == 0)
     class_kernel<0><<<blocks, 256, 0, st>>>(begA, begB, rows, min_deg, warp_max, cta_max, plain, rowmap, dec, ctl,
-                                            lists, off);
+                                            lists, off, row_lo, row_hi);
   else
     class_kernel<1><<<blocks, 256, 0, st>>>(begA, begB, rows, min_deg, warp_max, cta_max, plain, rowmap, dec, ctl,
-                                            lists, off);
+                                            lists, off, row_lo, row_hi);
   TC_NOTE_LAUNCH();
   TC_CUDA_TRY(cudaGetLastError());
   return TRUST_TC_OK;

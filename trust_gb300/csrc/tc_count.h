@@ -37,19 +37,24 @@ struct CountArgs {
   int dev_off;
   // huge rows up to this out-degree are counted by hub_kernel in shared memory (0: none)
   int hub_max_degree;
+  // failure-detection test: hub_kernel arms its copy barrier without issuing the copy and waits
+  // a few thousand cycles, so the bounded wait runs out with nothing in flight
+  int test_wait_expiry;
 };
 
 int launch_check(const int64_t *beg, const int32_t *adj, int64_t rows, int64_t m, int64_t id_bound,
                  int check_ids, TcControl *ctl, int num_sms, cudaStream_t st);
 // One CSR: validation + class histogram + scatter in one kernel; class c (>= 1) is listed at
 // lists[(c-1) rows ...] and class_count[c] is its size.  lists holds 7 rows entries.
+// Rows outside [row_lo, row_hi) (row_hi < 0: all rows) are validated but classed as skipped.
 int launch_check_classify(const int64_t *beg, const int32_t *adj, int64_t rows, int64_t m, int check_ids,
                           int min_deg, int warp_max, int cta_max, int schedule, TcControl *ctl, int *lists,
-                          int num_sms, cudaStream_t st);
+                          int num_sms, cudaStream_t st, int64_t row_lo = 0, int64_t row_hi = -1);
 int launch_classify(int pass, const int64_t *begA, const int64_t *begB, int64_t rows, int min_deg,
                     int warp_max, int cta_max, TcControl *ctl, int *lists, const ListOffsets &off,
                     int num_sms, cudaStream_t st, int schedule = TRUST_TC_SCHED_TUNED,
-                    const int *rowmap = nullptr, const unsigned char *dec = nullptr);
+                    const int *rowmap = nullptr, const unsigned char *dec = nullptr, int64_t row_lo = 0,
+                    int64_t row_hi = -1);
 // batches: graphs fall into TC_BATCH_CLASSES size classes, each with its own degree thresholds
 constexpr int TC_BATCH_CLASSES = 4;
 struct BatchThresholds {

@@ -95,6 +95,8 @@ struct DevGraph3 {
   int64_t max_deg_A;          // largest row of A when known (0: the validation pass's maximum)
   int split_ok;               // three distinct CSRs whose A and C rows are duplicate-free: the
                               // direction split may count an arc from C's side
+  int64_t row_lo, row_hi;     // one CSR: only arcs of source rows in [row_lo, row_hi) are counted
+                              // (row_hi = 0: all rows)
 };
 
 int ctx_init(trust_tc_ctx *c, int device);
@@ -119,8 +121,10 @@ struct SchedPlan {
   int64_t moved_arcs;               // pair slots the pass used (moved arcs and holes)
   bool overflow;                    // the pair arrays ran out (never expected): no split
 };
+// Only source rows in [row_lo, row_hi) are walked (their arcs planned and moved).
 int split_plan(trust_tc_ctx *c, const int64_t *beg, const int32_t *adj, int64_t n, int64_t m, cudaStream_t st,
-               const float *d_model, int warp_max, int cta_max, float promote_log2, int cta_warps, TcControl *ctl);
+               const float *d_model, int warp_max, int cta_max, float promote_log2, int cta_warps, TcControl *ctl,
+               int64_t row_lo, int64_t row_hi);
 // after the stream has synchronised
 void split_plan_read(const trust_tc_ctx *c, SchedPlan *plan);
 int radix_sort_u64(unsigned long long *keys, unsigned long long *tmp, int64_t n, const int *shifts, int nshifts,

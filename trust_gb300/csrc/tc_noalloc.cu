@@ -11,10 +11,14 @@
 // The array, g_noalloc_scratch, is TC_NOALLOC_SCRATCH_BYTES (16 MiB) of device memory that every
 // GPU which loads the library holds until the process exits.  Host code cannot use the symbol's
 // name as a device address, so the first call on each device looks its address up with
-// cudaGetSymbolAddress (with that device current) and caches it; make that first call before any
-// stream capture.  All calls share the array and leave their contents in it; the control block at
-// its start is cleared on the stream at the start of every call.  Calls that overlap on the GPU
-// (several streams or threads at once) race on the array and must be serialised by the caller.
+// cudaGetSymbolAddress (with that device current) and keeps it for the life of the process; make
+// that first call before any stream capture.  The kept address belongs to the device's primary
+// context: after cudaDeviceReset on that device the process must not call this entry point again.
+// All calls share the array and leave their contents in it; the control block at its start is
+// cleared on the stream at the start of every call.  Calls that overlap on the GPU (several
+// streams or threads at once) race on the array and must be serialised by the caller.  Each call
+// synchronises its stream twice (after classification, to size the class lists, and after the
+// count) and returns with the caller's current device unchanged.
 #include <algorithm>
 #include <mutex>
 
@@ -56,6 +60,17 @@ int ceil_log2_i64(int64_t x) {
 
 }  // namespace
 
+// Puts the caller's current device back when the call returns.
+struct DeviceRestore {
+  int prev = -1;
+  ~DeviceRestore() {
+    if (prev >= 0) cudaSetDevice(prev);
+  }
+};
+
+static int count_noalloc(const int64_t *d_begin, const int32_t *d_adj, int64_t n, int64_t m,
+                         const trust_tc_opts &o, trust_tc_result *r);
+
 extern "C" int trust_tc_count_csr_noalloc(const int64_t *d_begin, const int32_t *d_adj, int64_t n, int64_t m,
                                           const trust_tc_opts *opts, trust_tc_result *r) {
   if (!d_begin || !r || n < 0 || m < 0 || (m > 0 && !d_adj)) return TRUST_TC_E_ARG;
@@ -63,11 +78,22 @@ extern "C" int trust_tc_count_csr_noalloc(const int64_t *d_begin, const int32_t 
   trust_tc_opts o;
   if (opts) o = *opts; else trust_tc_opts_init(&o);
   if (o.ptr_kind != TRUST_TC_DEVICE) return TRUST_TC_E_UNSUPPORTED;
+  // per-vertex cycles would be written into a caller array this variant does not clear: refused
+  // rather than silently left untouched
+  if (o.record_cycles) return TRUST_TC_E_UNSUPPORTED;
+  if (o.row_begin || o.row_end) return TRUST_TC_E_UNSUPPORTED;  // row ranges: trust_tc_count_csr only
   uint64_t *cycles = r->vertex_cycles;
   *r = trust_tc_result();
   r->vertex_cycles = cycles;
   r->vertices = n;
   r->edges = m;
+  DeviceRestore restore;
+  TC_CUDA_TRY(cudaGetDevice(&restore.prev));
+  return count_noalloc(d_begin, d_adj, n, m, o, r);
+}
+
+static int count_noalloc(const int64_t *d_begin, const int32_t *d_adj, int64_t n, int64_t m,
+                         const trust_tc_opts &o, trust_tc_result *r) {
   int device = o.device;
   if (device < 0) TC_CUDA_TRY(cudaGetDevice(&device));
   TC_CUDA_TRY(cudaSetDevice(device));

@@ -47,10 +47,11 @@ constexpr int TC_SCHED_FLAT = 32;
 // Phase 1.  f(valid, v, d(v), u, d(u), pos, last) is called by all 32 lanes together (warp
 // collectives allowed); lanes with valid = false carry no arc.  pos = the arc's index in adj,
 // last = it ends its row.  Rows longer than TC_SCHED_FLAT are appended to longs[] (length in
-// *nlong) when longs is given.
+// *nlong) when longs is given.  Rows outside [row_lo, row_hi) are passed over.
 template <class F>
 __device__ __forceinline__ void short_arcs(const int64_t *__restrict__ beg, const int32_t *__restrict__ adj,
-                                           int64_t n, int *__restrict__ longs, unsigned long long *nlong, F f) {
+                                           int64_t n, int64_t row_lo, int64_t row_hi, int *__restrict__ longs,
+                                           unsigned long long *nlong, F f) {
   const int lane = threadIdx.x & 31;
   const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -58,7 +59,7 @@ __device__ __forceinline__ void short_arcs(const int64_t *__restrict__ beg, cons
   for (int64_t v0 = warp * 32; v0 < n; v0 += nwarps * 32) {
     const int64_t v = v0 + lane;
     int b = 0, dv = 0;
-    if (v < n) {
+    if (v < n && v >= row_lo && v < row_hi) {
       const long long lo = tc_ld_nc(beg + v);
       b = (int)lo;
       dv = (int)(tc_ld_nc(beg + v + 1) - lo);
@@ -273,16 +274,17 @@ enum { PLAN_W_ALL = 0, PLAN_W_MIN = 1, PLAN_SAVED = 2, PLAN_NLONG = 3, PLAN_NPAI
 // totals, the in-list count and work sum of every arc's target, the arcs the split would move
 // (as pairs), and the sortedness check; rows longer than TC_SCHED_FLAT are listed.
 __global__ void sched_short_kernel(const int64_t *__restrict__ beg, const int32_t *__restrict__ adj, int64_t n,
-                                   unsigned *__restrict__ cnt, unsigned long long *__restrict__ wsum,
-                                   unsigned long long *plans, int *__restrict__ longs, int2 *__restrict__ pairs,
-                                   unsigned long long pair_cap, TcControl *ctl) {
+                                   int64_t row_lo, int64_t row_hi, unsigned *__restrict__ cnt,
+                                   unsigned long long *__restrict__ wsum, unsigned long long *plans,
+                                   int *__restrict__ longs, int2 *__restrict__ pairs, unsigned long long pair_cap,
+                                   TcControl *ctl) {
   const int lane = threadIdx.x & 31;
   unsigned long long w_all = 0, w_min = 0;
   int bad = 0;
   PairBuf pb;
   pb.cap = pair_cap;
   pb.overflow = plans + PLAN_OVERFLOW;
-  short_arcs(beg, adj, n, longs, plans + PLAN_NLONG,
+  short_arcs(beg, adj, n, row_lo, row_hi, longs, plans + PLAN_NLONG,
              [&](bool valid, int v, int dv, int u, int du, int pos, bool last) {
                if (valid) {
                  w_all += (unsigned)du;
@@ -456,7 +458,8 @@ static size_t pair_slots(int64_t arcs, int64_t warps) {
 // predicted cycles and class decision plus the predicted saving of the split.  Enqueued only:
 // the totals reach the host with the stream's next synchronisation (split_plan_read).
 int split_plan(trust_tc_ctx *c, const int64_t *beg, const int32_t *adj, int64_t n, int64_t m, cudaStream_t st,
-               const float *d_model, int warp_max, int cta_max, float promote_log2, int cta_warps, TcControl *ctl) {
+               const float *d_model, int warp_max, int cta_max, float promote_log2, int cta_warps, TcControl *ctl,
+               int64_t row_lo, int64_t row_hi) {
   const size_t nn = (size_t)std::max<int64_t>(n + 1, 1);
   int rc = ensure((void **)&c->d_split_cnt, &c->split_cnt_cap, sizeof(unsigned) * nn);
   if (rc) return rc;
@@ -475,8 +478,9 @@ int split_plan(trust_tc_ctx *c, const int64_t *beg, const int32_t *adj, int64_t 
   TC_CUDA_TRY(cudaMemsetAsync(c->d_split_wsum, 0, sizeof(unsigned long long) * (size_t)(n + 1), st));
   TC_CUDA_TRY(cudaMemsetAsync(c->d_split_plans, 0, TC_PLAN_WORDS * sizeof(unsigned long long), st));
   float *sums = reinterpret_cast<float *>(c->d_split_plans + PLAN_SAVED);
-  sched_short_kernel<<<sb, 256, 0, st>>>(beg, adj, n, c->d_split_cnt, c->d_split_wsum, c->d_split_plans,
-                                         c->d_sched_long, c->d_split_pairs, slots, ctl);
+  if (row_hi <= 0) row_hi = n;
+  sched_short_kernel<<<sb, 256, 0, st>>>(beg, adj, n, row_lo, row_hi, c->d_split_cnt, c->d_split_wsum,
+                                         c->d_split_plans, c->d_sched_long, c->d_split_pairs, slots, ctl);
   TC_NOTE_LAUNCH();
   TC_CUDA_TRY(cudaGetLastError());
   if (d_model)

@@ -228,6 +228,7 @@ int trust_tc_count_tiles_device(const int64_t *d_begin, const int32_t *d_adj, in
     return TRUST_TC_E_ARG;
   trust_tc_opts o;
   if (opts) o = *opts; else trust_tc_opts_init(&o);
+  if (o.row_begin || o.row_end) return TRUST_TC_E_UNSUPPORTED;  // row ranges: single-graph calls only
   int rc = TRUST_TC_OK;
   {  // validate the whole CSR before the partition reads it
     trust_tc_ctx ctx;
@@ -273,6 +274,7 @@ int trust_tc_count_partitioned(const char *folder, int parts, const trust_tc_opt
   if (!folder || !r || parts < 1 || parts > 64) return TRUST_TC_E_ARG;
   trust_tc_opts o;
   if (opts) o = *opts; else trust_tc_opts_init(&o);
+  if (o.row_begin || o.row_end) return TRUST_TC_E_UNSUPPORTED;  // row ranges: single-graph calls only
   const int p = parts;
   std::vector<HostTile> ht((size_t)p * p);
   int rc = TRUST_TC_OK;
