@@ -736,7 +736,10 @@ def run_reference(args, ws, rank, local):
     line["cpu_baseline"]["single_core"] = single_core_counter(beg, adj)
     if w["kind"] != "batch":
         line["reference_preprocess"] = reference_preprocess(w)
-    if O.ref_kernel_available():
+    if not O.ref_kernel_available():
+        line["reference_kernel_sm103a"] = {"unavailable": "reference kernel cubin not built here (oracle/build_ref.sh "
+                                                          "needs the reference sources)"}
+    else:
         flags, _ = O.trust_check(beg, adj)
         if flags == O.TRUST_EXACT:
             try:

@@ -121,6 +121,22 @@ def test_rmat26_slices_match_oracle(rmat26):
             assert got["learned_split"].direction_split == 1, (lo, hi)
 
 
+def test_rmat26_whole_count_is_pinned(rmat26):
+    """The whole R-MAT 26 count equals the pinned count of the reference kernel itself (TC.cu
+    rebuilt for sm_103a) and, where its cubin is built, a fresh run of that kernel on this CSR."""
+    import json
+    beg, adj, hb, ha = rmat26
+    with open(os.path.join(os.path.dirname(__file__), "golden", "pinned_counts.json")) as f:
+        pin = json.load(f)["rmat26_ef32"]
+    assert (hb.size - 1, ha.size) == (pin["vertices"], pin["edges"])
+    with T.Context() as ctx:
+        assert T.count_csr(beg, adj, ctx=ctx).triangles == pin["triangles"]
+    if O.ref_kernel_available():
+        assert O.trust_check(hb, ha)[0] == O.TRUST_EXACT
+        ref, _ = O.ref_kernel_count(hb, ha, blocks=1024, chunk=1)
+        assert ref == pin["triangles"]
+
+
 def test_rmat26_slices_sum_to_whole(rmat26):
     beg, adj, hb, _ = rmat26
     n = hb.size - 1
