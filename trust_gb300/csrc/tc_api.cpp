@@ -383,9 +383,13 @@ int count_device(trust_tc_ctx *c, const DevGraph3 &g, const trust_tc_opts &o, bo
   // warp tables sized to the largest row a warp can get here (>= 128 slots: 4G for G32 groups)
   const int warp_slots = 1 << std::max(ceil_log2_size(2 * std::min<int64_t>(table_max, cfg.warp_max)), 7);
   size_t smem = (size_t)4 * warp_slots * (cfg.threads / 32);
+  // quotient tables for the CTA class when every key and probe id has at most 26 bits; the CTA
+  // table's bytes then also hold a 512-byte overflow list (tc_count.cu, TC_Q16_OVERFLOW)
+  const int key_bits = ceil_log2_size(std::max<int64_t>(std::max(g.boundA, g.boundC), 2));
+  const bool q16 = key_bits <= 26;
   if (h.class_count[TC_CLASS_CTA] > 0) {
     const int64_t dcta = std::min<int64_t>(h.max_out_degree, cfg.cta_max);
-    smem = std::max(smem, (size_t)4 << std::max(ceil_log2_size(2 * dcta), 6));
+    smem = std::max(smem, ((size_t)4 << std::max(ceil_log2_size(2 * dcta), 6)) + (q16 ? 512 : 0));
   }
   int blocks = cfg.blocks;
   {
@@ -419,6 +423,8 @@ int count_device(trust_tc_ctx *c, const DevGraph3 &g, const trust_tc_opts &o, bo
   a.split = split;
   a.rowmap = g.rowmap;
   a.test_wait_expiry = o.test_wait_expiry;
+  a.key_bits = q16 ? key_bits : 0;
+  a.cta_table_bytes = (int)smem;
   if (h.class_count[TC_CLASS_CTA] > 0) {
     // long-row lists: one per CTA, as long as the largest CTA-class row
     const int cap = (int)std::min<int64_t>(h.max_out_degree, cfg.cta_max);

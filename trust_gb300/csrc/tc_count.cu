@@ -86,6 +86,74 @@ struct HashSet {
   __device__ __forceinline__ int has(int w) const { return set_probe(tab, log2, w); }
 };
 
+// Quotient tables (CTA-class rows, shared memory): keys are ids below 2^kb (kb <= 26).  The map
+// h(k) = k * M mod 2^kb (M odd) is a bijection of [0, 2^kb), so a key is identified by the pair
+// (home bucket = top bb bits of h, remainder = low kb - bb bits) and a slot stores the remainder
+// alone: 16-bit slots (remainders <= 15 bits, 0xFFFF = empty), 8 per 16-byte bucket.  In the bytes
+// of a 32-bit table at half load the same row fills a quarter of the slots, so a home bucket is
+// full with probability about 0.1 % (2 keys per 8 slots on average) and a lookup is one 16-byte
+// load: no warp-divergent further rounds for the lanes whose bucket overflowed, which in 4-slot
+// buckets at half load hit nearly every warp (about a third of the count's time on R-MAT 26).
+// A remainder means something only in its home bucket, so a key whose home bucket is full goes,
+// whole, to a short overflow list after the buckets; a lookup reads that list only when its home
+// bucket is full.  Slots of a bucket fill in order (an insert takes the first free slot), so an
+// empty last slot means the bucket was never full.  If the list itself fills (not expected), the
+// row is rebuilt as a 32-bit table.
+constexpr unsigned TC_Q16_MULT = 0x9E3779B1u;
+constexpr int TC_Q16_MAX_KEY_BITS = 26;  // 2^(kb - 15) buckets must fit the CTA table's bytes
+constexpr int TC_Q16_OVERFLOW = 128;     // overflow list entries (512 bytes after the buckets)
+
+__device__ __forceinline__ unsigned q16_haszero(unsigned x) {  // some 16-bit half of x is 0
+  return (x - 0x00010001u) & ~x & 0x80008000u;
+}
+
+struct Q16Set {
+  const unsigned short *tab;
+  int bb;          // log2 buckets
+  int kb;          // key bits
+  const int *ov;   // keys whose home bucket was full
+  int n_ov;
+  __device__ __forceinline__ int has(int key) const {
+    const unsigned h = ((unsigned)key * TC_Q16_MULT) & ((1u << kb) - 1u);
+    const int rb = kb - bb;
+    const unsigned b = h >> rb;
+    const unsigned r = h & ((1u << rb) - 1u);
+    const unsigned rr = r | (r << 16);
+    const uint4 q = *reinterpret_cast<const uint4 *>(tab + 8 * b);
+    if (q16_haszero(q.x ^ rr) | q16_haszero(q.y ^ rr) | q16_haszero(q.z ^ rr) | q16_haszero(q.w ^ rr)) return 1;
+    if (q.w >= 0xFFFF0000u) return 0;  // last slot empty: the home bucket was never full
+    for (int i = 0; i < n_ov; ++i)
+      if (ov[i] == key) return 1;
+    return 0;
+  }
+};
+
+// Insert into the key's home bucket; false when that bucket is full (the caller lists the key).
+__device__ __forceinline__ bool q16_insert(unsigned short *tab, int bb, int kb, int key) {
+  const unsigned h = ((unsigned)key * TC_Q16_MULT) & ((1u << kb) - 1u);
+  const int rb = kb - bb;
+  const unsigned b = h >> rb;
+  const unsigned short r = (unsigned short)(h & ((1u << rb) - 1u));
+#pragma unroll 1
+  for (int j = 0; j < 8; ++j) {
+    const unsigned short prev = atomicCAS(tab + 8 * b + j, (unsigned short)0xFFFF, r);
+    if (prev == 0xFFFF || prev == r) return true;
+  }
+  return false;
+}
+
+// log2 buckets of a row of d keys in a quotient table: at least d/2 buckets (a quarter of the
+// slots used) and enough buckets that remainders fit 15 bits; -1 when the buckets and the
+// overflow list exceed the bytes available (the row takes a 32-bit table instead).
+__device__ __forceinline__ int q16_log2_buckets(int d, int kb, int table_bytes) {
+  if (kb <= 0 || kb > TC_Q16_MAX_KEY_BITS) return -1;
+  int bb = 0;
+  while ((1 << (bb + 1)) < d) ++bb;  // 2^(bb+1) >= d
+  bb = max(bb, kb - 15);
+  bb = min(bb, kb);
+  return (16 << bb) + 4 * TC_Q16_OVERFLOW <= table_bytes ? bb : -1;
+}
+
 constexpr int TC_UNROLL = 4;  // independent neighbour-row loads in flight per lane
 
 // Probe every wedge of the arcs held one per lane of a G-lane group against `set`.
@@ -551,6 +619,7 @@ struct BlockShared {
   int next_batch;
   int n_long;     // deferred long rows of the current CTA vertex
   int next_long;  // claim head over them
+  int n_ov;       // quotient table: keys in the overflow list
 };
 
 // Neighbour rows at least this long are set aside by the 32-arc batch pass of a CTA vertex and
@@ -633,27 +702,12 @@ __device__ __forceinline__ void batch_take(const CountArgs &p, BatchAcc &a, int 
 // Pass 1: warps claim 32-arc batches from a shared counter; short rows are flattened and probed
 // at once, rows of TC_CTA_LONG entries or more are appended to this CTA's long-row list (when
 // one is provided and the vertex fits it).  Pass 2: warps claim the long rows one at a time.
-template <bool SAME>
-__device__ void cta_vertex(const CountArgs &p, int v, int *tab, BlockShared &bs, unsigned long long &hits,
-                           unsigned long long &wedges) {
+// The arcs of a CTA vertex against its table (set): 32-arc batches claimed by the warps, then the
+// deferred long rows one per warp.
+template <class Set>
+__device__ __forceinline__ void cta_arcs(const CountArgs &p, const Set &set, int dA, int bB, int dB, BlockShared &bs,
+                                         unsigned long long &hits, unsigned long long &wedges) {
   const int lane = threadIdx.x & 31;
-  int bA, dA, bB, dB;
-  row_of(p.begA, arow(p, v), bA, dA);
-  if (SAME) { bB = bA; dB = dA; } else { row_of(p.begB, v, bB, dB); }
-  const int log2 = ceil_log2_table(dA);
-  const int T = 1 << log2;
-  for (int i = threadIdx.x; i < T; i += blockDim.x) tab[i] = -1;
-  if (threadIdx.x == 0) {
-    bs.next_batch = 0;
-    bs.n_long = 0;
-    bs.next_long = 0;
-  }
-  __syncthreads();
-  bool ok = true;
-  for (int i = threadIdx.x; i < dA; i += blockDim.x) ok &= set_insert(tab, log2, tc_ld_nc(p.adjA + bA + i));
-  if (!ok) atomicOr(&p.ctl->status, TC_DEV_TABLE_FULL);
-  __syncthreads();
-  const HashSet set{tab, log2};
   int2 *longs = (p.long_rows && dB <= p.long_cap) ? p.long_rows + (size_t)blockIdx.x * p.long_cap : nullptr;
   const int nbatch = (dB + 31) >> 5;
   for (;;) {
@@ -694,6 +748,52 @@ __device__ void cta_vertex(const CountArgs &p, int v, int *tab, BlockShared &bs,
     }
     __syncthreads();
   }
+}
+
+template <bool SAME>
+__device__ void cta_vertex(const CountArgs &p, int v, int *tab, bool smem_table, BlockShared &bs,
+                           unsigned long long &hits, unsigned long long &wedges) {
+  int bA, dA, bB, dB;
+  row_of(p.begA, arow(p, v), bA, dA);
+  if (SAME) { bB = bA; dB = dA; } else { row_of(p.begB, v, bB, dB); }
+  if (threadIdx.x == 0) {
+    bs.next_batch = 0;
+    bs.n_long = 0;
+    bs.next_long = 0;
+  }
+  const int bb = smem_table ? q16_log2_buckets(dA, p.key_bits, p.cta_table_bytes) : -1;
+  bool ok = true;
+  if (bb >= 0) {  // quotient table in shared memory, its overflow list after the buckets
+    unsigned *t32 = reinterpret_cast<unsigned *>(tab);
+    for (int i = threadIdx.x; i < (4 << bb); i += blockDim.x) t32[i] = 0xFFFFFFFFu;
+    if (threadIdx.x == 0) bs.n_ov = 0;
+    __syncthreads();
+    unsigned short *t16 = reinterpret_cast<unsigned short *>(tab);
+    int *ov = tab + (4 << bb);
+    for (int i = threadIdx.x; i < dA; i += blockDim.x) {
+      const int key = tc_ld_nc(p.adjA + bA + i);
+      if (!q16_insert(t16, bb, p.key_bits, key)) {
+        const int at = atomicAdd(&bs.n_ov, 1);
+        if (at < TC_Q16_OVERFLOW) ov[at] = key;
+      }
+    }
+    __syncthreads();
+    const int n_ov = bs.n_ov;
+    if (n_ov <= TC_Q16_OVERFLOW) {
+      cta_arcs(p, Q16Set{t16, bb, p.key_bits, ov, n_ov}, dA, bB, dB, bs, hits, wedges);
+      return;
+    }
+    // the overflow list ran out: the 32-bit table below (every thread has read n_ov; nothing
+    // reads the quotient table any more)
+  }
+  const int log2 = ceil_log2_table(dA);
+  const int T = 1 << log2;
+  for (int i = threadIdx.x; i < T; i += blockDim.x) tab[i] = -1;
+  __syncthreads();
+  for (int i = threadIdx.x; i < dA; i += blockDim.x) ok &= set_insert(tab, log2, tc_ld_nc(p.adjA + bA + i));
+  if (!ok) atomicOr(&p.ctl->status, TC_DEV_TABLE_FULL);
+  __syncthreads();
+  cta_arcs(p, HashSet{tab, log2}, dA, bB, dB, bs, hits, wedges);
 }
 
 // One vertex per warp, 32 < out-degree <= warp_max: several 32-arc rounds on a warp table.
@@ -883,7 +983,7 @@ __global__ void __launch_bounds__(MAXT, MINB) count_kernel(CountArgs p) {
       }
       const long long t_start = REC ? clock64() : 0;
       const unsigned long long h0 = hits;
-      cta_vertex<SAME>(p, v, tab, bs, hits, wedges);
+      cta_vertex<SAME>(p, v, tab, c == TC_CLASS_CTA, bs, hits, wedges);
       if (REC && threadIdx.x == 0) p.cycles[v] = (unsigned long long)(clock64() - t_start);
       if constexpr (BATCH) batch_take(p, acc, p.graph_of[v], hits - h0);
     }

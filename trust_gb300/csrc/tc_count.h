@@ -40,6 +40,10 @@ struct CountArgs {
   // failure-detection test: hub_kernel arms its copy barrier without issuing the copy and waits
   // a few thousand cycles, so the bounded wait runs out with nothing in flight
   int test_wait_expiry;
+  // CTA-class tables: every key (entry of A) and probe (entry of C) is below 2^key_bits (0: no
+  // quotient tables), and the CTA table may use cta_table_bytes of dynamic shared memory
+  int key_bits;
+  int cta_table_bytes;
 };
 
 int launch_check(const int64_t *beg, const int32_t *adj, int64_t rows, int64_t m, int64_t id_bound,

@@ -162,7 +162,6 @@ int tile_loop(const std::vector<HostTile> &ht, int p, const trust_tc_opts &o, si
   double tk = 0, tcount = 0;
   int64_t n_total = 0;
   for (int i = 0; i < p; ++i) n_total += ht[(size_t)i * p].rows;
-  const int64_t NOBOUND = ((int64_t)1 << 31) - 1;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
@@ -180,7 +179,10 @@ int tile_loop(const std::vector<HostTile> &ht, int p, const trust_tc_opts &o, si
         g.rows = ht[A].rows;
         g.rowsC = ht[C].rows;
         g.mA = ht[A].m; g.mB = ht[Bt].m; g.mC = ht[C].m;
-        g.boundA = NOBOUND; g.boundB = ht[C].rows; g.boundC = NOBOUND;
+        // entries of tiles (i,j) and (k,j) are local ids of column class j, below the row count of
+        // tile row class j (validated by the job's id check)
+        g.boundA = g.boundC = ht[(size_t)j * p].rows;
+        g.boundB = ht[C].rows;
         // a diagonal job (i,i,i) is one CSR: rows with one entry close no triangle there
         g.min_deg = (A == Bt && Bt == C) ? 2 : 1;
         g.split_ok = increasing[A] == 1 && increasing[C] == 1;
