@@ -627,25 +627,44 @@ struct BlockShared {
 constexpr int TC_CTA_LONG = 256;
 
 // Walk one neighbour row with a whole warp: 32 * TC_UNROLL entries per step, next step's loads
-// issued before the current step is probed.
+// issued before the current step is probed.  Steps that lie wholly inside the row take no bounds
+// test; the hits of the row are summed in 32 bits (a row has fewer than 2^26 entries).
 template <class Set>
 __device__ __forceinline__ void walk_row_warp(const int32_t *__restrict__ row, int dj, int lane, const Set &set,
                                               unsigned long long &hits) {
   constexpr int U = TC_UNROLL;
-  int w[U];
+  constexpr int STEP = 32 * U;
+  unsigned h = 0;
+  int k0 = 0;
+  if (dj >= STEP) {
+    int w[U];
 #pragma unroll
-  for (int r = 0; r < U; ++r) w[r] = lane + r * 32 < dj ? tc_ld_nc(row + lane + r * 32) : -1;
-  for (int k = lane; k < dj; k += 32 * U) {
-    const int kn = k + 32 * U;
-    int wn[U];
+    for (int r = 0; r < U; ++r) w[r] = tc_ld_nc(row + lane + r * 32);
+    for (; k0 + 2 * STEP <= dj; k0 += STEP) {
+      int wn[U];
 #pragma unroll
-    for (int r = 0; r < U; ++r) wn[r] = kn + r * 32 < dj ? tc_ld_nc(row + kn + r * 32) : -1;
+      for (int r = 0; r < U; ++r) wn[r] = tc_ld_nc(row + k0 + STEP + lane + r * 32);
+#pragma unroll
+      for (int r = 0; r < U; ++r) h += set.has(w[r]);
+#pragma unroll
+      for (int r = 0; r < U; ++r) w[r] = wn[r];
+    }
+#pragma unroll
+    for (int r = 0; r < U; ++r) h += set.has(w[r]);
+    k0 += STEP;
+  }
+  if (k0 < dj) {  // the last, partial step
+    int w[U];
+#pragma unroll
+    for (int r = 0; r < U; ++r) {
+      const int k = k0 + lane + r * 32;
+      w[r] = k < dj ? tc_ld_nc(row + k) : -1;
+    }
 #pragma unroll
     for (int r = 0; r < U; ++r)
-      if (w[r] >= 0) hits += set.has(w[r]);
-#pragma unroll
-    for (int r = 0; r < U; ++r) w[r] = wn[r];
+      if (w[r] >= 0) h += set.has(w[r]);
   }
+  hits += h;
 }
 
 __device__ __forceinline__ int ceil_log2_table(int d) {
@@ -1133,13 +1152,16 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned pari
 // memory is not released under a write still landing.  With p.test_wait_expiry the barrier is
 // armed without a copy, so the wait runs out with nothing in flight.
 template <bool SAME>
-__global__ void __launch_bounds__(512, 1) hub_kernel(CountArgs p, int log2C, int share_log2_max) {
+__global__ void __launch_bounds__(512, 2) hub_kernel(CountArgs p, int log2C, int share_log2_max) {
   extern __shared__ __align__(16) int smem[];
   __shared__ int next_batch;
   __shared__ __align__(8) unsigned long long bar;
   __shared__ int tma_ok;
   __shared__ int abandoned;  // 1 + parity of a barrier phase whose copy this CTA stopped waiting for
-  int *stage = smem + (1 << share_log2_max);
+  __shared__ int n_ov;       // quotient table: keys in the overflow list
+  // dynamic shared memory: the table share, the quotient table's overflow list, the staging buffer
+  int *ov = smem + (1 << share_log2_max);
+  int *stage = ov + TC_Q16_OVERFLOW;
   if (threadIdx.x == 0) {
     mbar_init(&bar);
     tma_ok = ((reinterpret_cast<uintptr_t>(p.adjA) & 15) == 0);  // 16-byte aligned base: copy the interior
@@ -1167,10 +1189,26 @@ __global__ void __launch_bounds__(512, 1) hub_kernel(CountArgs p, int log2C, int
     const int log2 = ceil_log2_table(dA);
     const DsmemSet set{smem, log2, log2 - log2C};
     const int share = 1 << (log2 - log2C);
-    for (int i = threadIdx.x; i < share; i += blockDim.x) smem[i] = -1;
+    // one CTA: a quotient table (see Q16Set) when the ids allow it, else the 32-bit table
+    const int bb = log2C == 0 ? q16_log2_buckets(dA, p.key_bits, (4 << share_log2_max) + 4 * TC_Q16_OVERFLOW) : -1;
+    unsigned short *t16 = reinterpret_cast<unsigned short *>(smem);
+    if (bb >= 0) {
+      for (int i = threadIdx.x; i < (4 << bb); i += blockDim.x) smem[i] = -1;
+    } else {
+      for (int i = threadIdx.x; i < share; i += blockDim.x) smem[i] = -1;
+    }
+    if (threadIdx.x == 0) n_ov = 0;
     if (rank == 0 && threadIdx.x == 0) next_batch = 0;
     cl.sync();
     bool ok = true;
+    auto insert = [&](int key) -> bool {
+      if (bb < 0) return set.insert(key);
+      if (!q16_insert(t16, bb, p.key_bits, key)) {
+        const int at = atomicAdd(&n_ov, 1);
+        if (at < TC_Q16_OVERFLOW) ov[at] = key;
+      }
+      return true;
+    };
     {  // this CTA's share of the row: entries [lo, hi)
       const int per = (dA + C - 1) >> log2C;
       const int lo = min(rank * per, dA), hi = min(lo + per, dA);
@@ -1182,15 +1220,15 @@ __global__ void __launch_bounds__(512, 1) hub_kernel(CountArgs p, int log2C, int
           if (copy) bulk_copy_g2s(stage, p.adjA + i0, (unsigned)(i1 - i0) * 4u, &bar);
           else mbar_arm(&bar, (unsigned)(i1 - i0) * 4u);  // nothing will arrive
         }
-        for (long long i = a0 + threadIdx.x; i < i0; i += blockDim.x) ok &= set.insert(tc_ld_nc(p.adjA + i));
-        for (long long i = i1 + threadIdx.x; i < a1; i += blockDim.x) ok &= set.insert(tc_ld_nc(p.adjA + i));
+        for (long long i = a0 + threadIdx.x; i < i0; i += blockDim.x) ok &= insert(tc_ld_nc(p.adjA + i));
+        for (long long i = i1 + threadIdx.x; i < a1; i += blockDim.x) ok &= insert(tc_ld_nc(p.adjA + i));
         const bool arrived = mbar_wait(&bar, parity, copy ? TC_WAIT_CYCLES : TC_TEST_WAIT_CYCLES);
         parity ^= 1u;
         if (arrived) {
-          for (int i = threadIdx.x; i < (int)(i1 - i0); i += blockDim.x) ok &= set.insert(stage[i]);
+          for (int i = threadIdx.x; i < (int)(i1 - i0); i += blockDim.x) ok &= insert(stage[i]);
         } else {  // give up on the copy: report it and read the interior directly
           if (threadIdx.x == 0) atomicOr(&p.ctl->status, TC_DEV_WAIT_LIMIT);
-          for (long long i = i0 + threadIdx.x; i < i1; i += blockDim.x) ok &= set.insert(tc_ld_nc(p.adjA + i));
+          for (long long i = i0 + threadIdx.x; i < i1; i += blockDim.x) ok &= insert(tc_ld_nc(p.adjA + i));
         }
         __syncthreads();  // the staging buffer is free again, and every thread saw the same outcome
         if (threadIdx.x == 0 && !arrived) {
@@ -1199,23 +1237,37 @@ __global__ void __launch_bounds__(512, 1) hub_kernel(CountArgs p, int log2C, int
         }
         __syncthreads();
       } else {
-        for (long long i = a0 + threadIdx.x; i < a1; i += blockDim.x) ok &= set.insert(tc_ld_nc(p.adjA + i));
+        for (long long i = a0 + threadIdx.x; i < a1; i += blockDim.x) ok &= insert(tc_ld_nc(p.adjA + i));
       }
     }
     if (!ok) atomicOr(&p.ctl->status, TC_DEV_TABLE_FULL);
     cl.sync();
-    const int nbatch = (dB + 31) >> 5;
-    for (;;) {
-      int bt = 0;
-      if (lane == 0) bt = atomicAdd(ctr, 1);
-      bt = __shfl_sync(TC_FULL_MASK, bt, 0);
-      if (bt >= nbatch) break;
-      const int i = (bt << 5) + lane;
-      int s = 0, dd = 0;
-      if (i < dB) row_of(p.begC, tc_ld_nc(p.adjB + bB + i), s, dd);
-      if (p.split && dd > dA) dd = 0;
-      probe_arcs<32, LongRow<32>::value>(p.adjC, s, dd, lane, set, hits, wedges);
+    bool use16 = bb >= 0;
+    if (use16 && n_ov > TC_Q16_OVERFLOW) {  // the overflow list ran out (one CTA): a 32-bit table
+      use16 = false;
+      __syncthreads();
+      for (int i = threadIdx.x; i < share; i += blockDim.x) smem[i] = -1;
+      __syncthreads();
+      for (int i = threadIdx.x; i < dA; i += blockDim.x) ok &= set.insert(tc_ld_nc(p.adjA + bA + i));
+      if (!ok) atomicOr(&p.ctl->status, TC_DEV_TABLE_FULL);
+      __syncthreads();
     }
+    auto probe_all = [&](const auto &tset) {
+      const int nbatch = (dB + 31) >> 5;
+      for (;;) {
+        int bt = 0;
+        if (lane == 0) bt = atomicAdd(ctr, 1);
+        bt = __shfl_sync(TC_FULL_MASK, bt, 0);
+        if (bt >= nbatch) break;
+        const int i = (bt << 5) + lane;
+        int s = 0, dd = 0;
+        if (i < dB) row_of(p.begC, tc_ld_nc(p.adjB + bB + i), s, dd);
+        if (p.split && dd > dA) dd = 0;
+        probe_arcs<32, LongRow<32>::value>(p.adjC, s, dd, lane, tset, hits, wedges);
+      }
+    };
+    if (use16) probe_all(Q16Set{t16, bb, p.key_bits, ov, n_ov});
+    else probe_all(set);
     cl.sync();  // every probe of this hub is done before any share is cleared again
     if (p.cycles && rank == 0 && threadIdx.x == 0) p.cycles[v] = (unsigned long long)(clock64() - t_start);
   }
@@ -1265,7 +1317,7 @@ int launch_hub(bool same, const CountArgs &a, int max_log2, int log2C, int clust
   // table share + staging for one CTA's share of the longest row (plus alignment slack)
   const int share_log2 = max_log2 - log2C;
   const size_t stage_ints = (((size_t)a.hub_max_degree + (1u << log2C) - 1) >> log2C) + 8;
-  const size_t smem = ((size_t)4 << share_log2) + 4 * stage_ints;
+  const size_t smem = ((size_t)4 << share_log2) + 4 * (size_t)TC_Q16_OVERFLOW + 4 * stage_ints;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)(clusters << log2C));
   cfg.blockDim = dim3(512);
