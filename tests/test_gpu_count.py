@@ -420,3 +420,24 @@ def test_row_range_slices(ctx):
     for bad in ((-1, 5), (6, 5), (0, n + 1)):
         with pytest.raises(T.TrustTcError):
             T.count_csr(beg, adj, ctx=ctx, row_range=bad)
+
+
+def test_small_skewed_graphs_take_the_plain_split(ctx):
+    """Under the default schedule a graph of fewer than 2^21 arcs with a row of at least 64 entries
+    is counted with the plain split (one warp per row up to 100 entries, a CTA above), which is
+    faster there; a small graph without long rows keeps the sub-warp classes.  Counts never change."""
+    pairs = T.gen_rmat(16, 16, seed=1)
+    beg, adj = T.build_csr(pairs, 1 << 16)
+    d = np.diff(beg.cpu().numpy())
+    default = T.count_csr(beg, adj, ctx=ctx)
+    plain = T.count_csr(beg, adj, ctx=ctx, schedule=T.SCHED_PLAIN)
+    assert default.triangles == plain.triangles
+    assert default.class_sizes == plain.class_sizes
+    assert default.class_sizes["warp"] == int(np.sum((d >= 2) & (d <= 100)))
+    tuned = T.count_csr(beg, adj, ctx=ctx, schedule=T.SCHED_TUNED)
+    assert tuned.triangles == default.triangles and tuned.class_sizes["g4"] > 0
+    pairs = T.gen_chung_lu(200_000, 2.5, 300.0, 800_000, 800_000, seed=11)
+    beg, adj = T.build_csr(pairs, 200_000)
+    assert int((beg[1:] - beg[:-1]).max()) < 64
+    default = T.count_csr(beg, adj, ctx=ctx)
+    assert default.class_sizes == T.count_csr(beg, adj, ctx=ctx, schedule=T.SCHED_TUNED).class_sizes

@@ -51,12 +51,17 @@ def test_noalloc_matches_regular_entry_point_twice():
     for name, beg, adj in _graphs():
         rc, ref = _regular(beg, adj)
         assert rc == _lib.OK, name
+        # the allocation-free variant always lists the sub-warp classes; the regular entry point's
+        # default may take the plain split on a small skewed graph, so classes are compared with
+        # the regular entry point under the tuned schedule
+        rc, ref_tuned = _regular(beg, adj, schedule=T.SCHED_TUNED)
+        assert rc == _lib.OK, name
         for call in range(2):
             rc, r = _noalloc(beg, adj)
             assert rc == _lib.OK, (name, call, rc)
             assert r.triangles == ref.triangles, (name, call)
             assert r.wedges == ref.wedges and r.max_out_degree == ref.max_out_degree, (name, call)
-            assert list(r.class_sizes) == list(ref.class_sizes), (name, call)
+            assert list(r.class_sizes) == list(ref_tuned.class_sizes), (name, call)
 
 
 def test_noalloc_rejects_what_it_cannot_hold():

@@ -179,6 +179,14 @@ constexpr int64_t TC_LEARNED_MIN_ARCS = (int64_t)1 << 22;
 // (scales 18-21; 34-67 % of arcs in such rows) and lost on a = 0.45 R-MAT and Chung-Lu graphs
 // (0-6 %), where the pass alone cost 0.3-1.0 ms more than the tuned classes.
 constexpr double TC_LEARNED_MIN_LONG_FRAC = 0.15;
+// Small graphs with long rows (fewer than 2^21 arcs, a row of at least 64 entries) run the plain
+// split, in 128-thread CTAs, under the learned schedule: packing 4 to 32 rows per warp leaves too few warp tasks to
+// fill the GPU while the long rows hold their warps.  Measured on GB300 (call ms, default tuned
+// classes vs plain): R-MAT 14 0.222 / 0.155, R-MAT 16 0.450 / 0.421, R-MAT 17 0.812 / 0.728, while
+// from R-MAT 18 (3.8M arcs: 1.62 / 1.67) and on small Chung-Lu, Erdos-Renyi and Barabasi-Albert
+// graphs (longest rows 18 to 29 entries: 0.09 / 0.20, 0.11 / 0.14, 0.09 / 0.12) the tuned classes win.
+constexpr int64_t TC_SMALL_SKEWED_ARCS = (int64_t)1 << 21;
+constexpr int TC_SMALL_SKEWED_MIN_ROW = 64;
 
 // Make the cost model in use resident on the device: the caller's (opts.model) or the library's
 // default.  Sets *d_model to null when neither is available (no decisions from a model).
@@ -230,12 +238,19 @@ int count_device(trust_tc_ctx *c, const DevGraph3 &g, const trust_tc_opts &o, bo
   // one CSR: validation, class histogram and list scatter in one kernel, each class listed in a
   // fixed range of the list buffer (7 rows entries), so no offsets wait for the host
   const bool fused = same && !g.rowmap && 7 * g.rows < ((int64_t)1 << 31);
+  // a small graph under the default learned schedule is listed under the plain split as well (the
+  // second 7 rows entries), so the host can take it after the one readback
+  const bool small_alt = fused && o.schedule == TRUST_TC_SCHED_LEARNED && o.warp_max_degree <= 0 &&
+                         o.direction_split != 1 && g.min_deg == 2 && g.mA < TC_SMALL_SKEWED_ARCS &&
+                         14 * g.rows < ((int64_t)1 << 31);
   if (fused) {
-    rc = ensure((void **)&c->d_lists, &c->lists_cap, sizeof(int) * (size_t)std::max<int64_t>(7 * g.rows, 1));
+    rc = ensure((void **)&c->d_lists, &c->lists_cap,
+                sizeof(int) * (size_t)std::max<int64_t>((small_alt ? 14 : 7) * g.rows, 1));
     if (rc) return rc;
     TC_CUDA_TRY(cudaEventRecord(c->ev[1], st));
     rc = launch_check_classify(g.begA, g.adjA, g.rows, g.mA, check_ids, g.min_deg, cfg.warp_max, cfg.cta_max,
-                               o.schedule, ctl, c->d_lists, c->num_sms, st, row_lo, row_hi);
+                               o.schedule, ctl, c->d_lists, c->num_sms, st, row_lo, row_hi,
+                               small_alt ? c->d_lists + 7 * g.rows : nullptr);
     if (rc) return rc;
   } else {
     // 1. validation of every distinct CSR: offsets always, ids on request
@@ -262,6 +277,18 @@ int count_device(trust_tc_ctx *c, const DevGraph3 &g, const trust_tc_opts &o, bo
   if (h.status & TC_DEV_BAD_OFFSETS) return TRUST_TC_E_OFFSETS;
   if (h.status & TC_DEV_TOO_LARGE) return TRUST_TC_E_TOO_LARGE;
   if (h.status & TC_DEV_BAD_IDS) return TRUST_TC_E_IDS;
+  const bool plain_small = small_alt && h.max_out_degree >= TC_SMALL_SKEWED_MIN_ROW;
+  if (plain_small) {
+    // the kernels read every class's size from the device control block: it must hold the plain
+    // split's sizes too, or they would walk past the ends of the plain lists
+    memcpy(h.class_count, h.class_count_alt, sizeof h.class_count);
+    TC_CUDA_TRY(cudaMemcpyAsync(ctl->class_count, ctl->class_count_alt, sizeof ctl->class_count,
+                                cudaMemcpyDeviceToDevice, st));
+    cfg.warp_max = TC_PLAIN_WARP_MAX;
+    // and 128-thread CTAs unless the caller chose: R-MAT 16 0.377 ms against 0.423 with 256, R-MAT
+    // 17 0.686 against 0.733 (GB300); the grid is sized from the occupancy of this shape below
+    if (o.threads_per_block <= 0) cfg.threads = 128;
+  }
   // Learned schedule: one scheduling pass over the arcs (split plan, and with a cost model the
   // predicted cycles and class decision of every row longer than 32), then the direction split
   // decision; the decisions re-run the class histogram.
@@ -338,7 +365,7 @@ int count_device(trust_tc_ctx *c, const DevGraph3 &g, const trust_tc_opts &o, bo
   const bool lists_done = fused && !dec;
   int64_t total = 0;
   for (int k = TC_CLASS_SKIP + 1; k < TC_NUM_CLASSES; ++k) {
-    off.off[k] = lists_done ? (int)((k - 1) * g.rows) : (int)total;
+    off.off[k] = lists_done ? (int)((plain_small ? 7 + k - 1 : k - 1) * g.rows) : (int)total;
     total += h.class_count[k];
   }
   if (!lists_done) {

@@ -46,6 +46,7 @@ struct TcControl {
   int class_next[TC_NUM_CLASSES];     // work-queue heads (atomic chunk claims)
   int class_off[TC_NUM_CLASSES];      // list offsets, when computed on the device (batches)
   unsigned long long long_arcs;       // arcs of rows longer than TC_LONG_ROW (single-graph calls)
+  int class_count_alt[TC_NUM_CLASSES];  // small graphs: list sizes under the plain split as well
 };
 constexpr int TC_LONG_ROW = 128;
 

@@ -459,7 +459,10 @@ __global__ void class_kernel(const int64_t *__restrict__ begA, const int64_t *__
 // class, and scatters from the classes kept in registers.  Rows with bad offsets are flagged and
 // left out of every list.  The id check is a separate grid-strided stream over adj.  Rows outside
 // [row_lo, row_hi) are validated and measured (maximum out-degree, arcs in long rows) but listed
-// in no class: their arcs are not counted.
+// in no class: their arcs are not counted.  With alt_lists, every row is also classed under the
+// plain split (warp up to TC_PLAIN_WARP_MAX entries, CTA above) and listed there (class c at
+// [(c-1) rows, c rows) of alt_lists, sizes in class_count_alt): the host then picks one of the
+// two classifications after its one readback, with no second pass.
 constexpr int TC_CC_THREADS = 256;
 constexpr int TC_CC_PER = 8;
 constexpr int TC_CC_ROWS = TC_CC_THREADS * TC_CC_PER;
@@ -467,14 +470,16 @@ constexpr int TC_CC_ROWS = TC_CC_THREADS * TC_CC_PER;
 __global__ void __launch_bounds__(TC_CC_THREADS) check_class_kernel(
     const int64_t *__restrict__ beg, const int32_t *__restrict__ adj, int64_t rows, int64_t m, int check_ids,
     int min_deg, int warp_max, int cta_max, int plain, TcControl *ctl, int *__restrict__ lists, int64_t row_lo,
-    int64_t row_hi) {
+    int64_t row_hi, int *__restrict__ alt_lists) {
   __shared__ int s_hist[TC_NUM_CLASSES];
   __shared__ int s_base[TC_NUM_CLASSES];
+  __shared__ int s_hist2[TC_NUM_CLASSES];
+  __shared__ int s_base2[TC_NUM_CLASSES];
   const unsigned lt = tc_lanemask_lt();
   const int64_t r0 = (int64_t)blockIdx.x * TC_CC_ROWS;
   int bad = 0, dmax = 0;
   unsigned long long long_arcs = 0;
-  if (threadIdx.x < TC_NUM_CLASSES) s_hist[threadIdx.x] = 0;
+  if (threadIdx.x < TC_NUM_CLASSES) s_hist[threadIdx.x] = s_hist2[threadIdx.x] = 0;
   long long lo[TC_CC_PER], hi[TC_CC_PER];
 #pragma unroll
   for (int k = 0; k < TC_CC_PER; ++k) {
@@ -482,9 +487,10 @@ __global__ void __launch_bounds__(TC_CC_THREADS) check_class_kernel(
     lo[k] = v < rows ? tc_ld_nc(beg + v) : 0;
     hi[k] = v < rows ? tc_ld_nc(beg + v + 1) : 0;
   }
-  int cls[TC_CC_PER];
+  int cls[TC_CC_PER], cls2[TC_CC_PER];
 #pragma unroll
   for (int k = 0; k < TC_CC_PER; ++k) {
+    cls2[k] = -1;
     const int64_t v = r0 + k * TC_CC_THREADS + threadIdx.x;
     int c = -1;
     if (v < rows) {
@@ -497,6 +503,8 @@ __global__ void __launch_bounds__(TC_CC_THREADS) check_class_kernel(
         dmax = max(dmax, d);
         if (d > TC_LONG_ROW) long_arcs += (unsigned)d;
         c = (v >= row_lo && v < row_hi) ? classify(d, d, min_deg, warp_max, cta_max, plain) : TC_CLASS_SKIP;
+        if (alt_lists)
+          cls2[k] = (v >= row_lo && v < row_hi) ? classify(d, d, min_deg, TC_PLAIN_WARP_MAX, cta_max, 1) : TC_CLASS_SKIP;
       }
     }
     cls[k] = c;
@@ -506,11 +514,20 @@ __global__ void __launch_bounds__(TC_CC_THREADS) check_class_kernel(
   for (int k = 0; k < TC_CC_PER; ++k) {
     const unsigned peers = __match_any_sync(TC_FULL_MASK, cls[k]);
     if (cls[k] >= 0 && (peers & lt) == 0) atomicAdd(&s_hist[cls[k]], __popc(peers));
+    if (alt_lists) {
+      const unsigned peers2 = __match_any_sync(TC_FULL_MASK, cls2[k]);
+      if (cls2[k] >= 0 && (peers2 & lt) == 0) atomicAdd(&s_hist2[cls2[k]], __popc(peers2));
+    }
   }
   __syncthreads();
   if (threadIdx.x < TC_NUM_CLASSES) {
     s_base[threadIdx.x] = s_hist[threadIdx.x] ? atomicAdd(&ctl->class_count[threadIdx.x], s_hist[threadIdx.x]) : 0;
     s_hist[threadIdx.x] = 0;  // from here on: this block's fill cursor per class
+    if (alt_lists) {
+      s_base2[threadIdx.x] =
+          s_hist2[threadIdx.x] ? atomicAdd(&ctl->class_count_alt[threadIdx.x], s_hist2[threadIdx.x]) : 0;
+      s_hist2[threadIdx.x] = 0;
+    }
   }
   __syncthreads();
 #pragma unroll
@@ -522,6 +539,16 @@ __global__ void __launch_bounds__(TC_CC_THREADS) check_class_kernel(
     at = __shfl_sync(TC_FULL_MASK, at, __ffs(peers) - 1);
     if (c > TC_CLASS_SKIP)
       lists[(int64_t)(c - 1) * rows + s_base[c] + at + __popc(peers & lt)] = (int)(r0 + k * TC_CC_THREADS + threadIdx.x);
+    if (alt_lists) {
+      const int c2 = cls2[k];
+      const unsigned peers2 = __match_any_sync(TC_FULL_MASK, c2);
+      int at2 = 0;
+      if (c2 > TC_CLASS_SKIP && (peers2 & lt) == 0) at2 = atomicAdd(&s_hist2[c2], __popc(peers2));
+      at2 = __shfl_sync(TC_FULL_MASK, at2, __ffs(peers2) - 1);
+      if (c2 > TC_CLASS_SKIP)
+        alt_lists[(int64_t)(c2 - 1) * rows + s_base2[c2] + at2 + __popc(peers2 & lt)] =
+            (int)(r0 + k * TC_CC_THREADS + threadIdx.x);
+    }
   }
   const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (tid == 0 && (tc_ld_nc(beg) != 0 || tc_ld_nc(beg + rows) != m)) bad |= TC_DEV_BAD_OFFSETS;
@@ -626,13 +653,15 @@ struct BlockShared {
 // then claimed one row per warp, so one batch full of long rows no longer holds up the CTA.
 constexpr int TC_CTA_LONG = 256;
 
-// Walk one neighbour row with a whole warp: 32 * TC_UNROLL entries per step, next step's loads
-// issued before the current step is probed.  Steps that lie wholly inside the row take no bounds
-// test; the hits of the row are summed in 32 bits (a row has fewer than 2^26 entries).
+// Walk one neighbour row with a whole warp: 32 * 2 TC_UNROLL entries per step, next step's loads
+// issued before the current step is probed (R-MAT 26: 4 % faster than 4 loads per lane, the bytes
+// in flight bounding the walks of rows read from anywhere in the graph).  Steps that lie wholly
+// inside the row take no bounds test; the hits of the row are summed in 32 bits (a row has fewer
+// than 2^26 entries).
 template <class Set>
 __device__ __forceinline__ void walk_row_warp(const int32_t *__restrict__ row, int dj, int lane, const Set &set,
                                               unsigned long long &hits) {
-  constexpr int U = TC_UNROLL;
+  constexpr int U = 2 * TC_UNROLL;  // eight loads in flight per lane: long walks are bound by bytes in flight
   constexpr int STEP = 32 * U;
   unsigned h = 0;
   int k0 = 0;
@@ -1359,14 +1388,14 @@ int launch_check(const int64_t *beg, const int32_t *adj, int64_t rows, int64_t m
 
 int launch_check_classify(const int64_t *beg, const int32_t *adj, int64_t rows, int64_t m, int check_ids,
                           int min_deg, int warp_max, int cta_max, int schedule, TcControl *ctl, int *lists,
-                          int num_sms, cudaStream_t st, int64_t row_lo, int64_t row_hi) {
+                          int num_sms, cudaStream_t st, int64_t row_lo, int64_t row_hi, int *alt_lists) {
   // one block per TC_CC_ROWS rows; blocks past the last row only check ids (few rows, many arcs)
   int64_t blocks = std::max<int64_t>(1, (rows + TC_CC_ROWS - 1) / TC_CC_ROWS);
   if (check_ids) blocks = std::max<int64_t>(blocks, std::min<int64_t>((m + 4095) / 4096, (int64_t)num_sms * 8));
   if (blocks > 0x7fffffff) return TRUST_TC_E_TOO_LARGE;
   check_class_kernel<<<(unsigned)blocks, TC_CC_THREADS, 0, st>>>(beg, adj, rows, m, check_ids, min_deg, warp_max,
                                                                  cta_max, schedule == TRUST_TC_SCHED_PLAIN, ctl, lists,
-                                                                 row_lo, row_hi < 0 ? rows : row_hi);
+                                                                 row_lo, row_hi < 0 ? rows : row_hi, alt_lists);
   TC_NOTE_LAUNCH();
   TC_CUDA_TRY(cudaGetLastError());
   return TRUST_TC_OK;

@@ -4,6 +4,9 @@
 
 namespace tc {
 
+// The plain split's warp bound: the reference's USE_CTA (Without-graph-partition/TC.cu:19).
+constexpr int TC_PLAIN_WARP_MAX = 100;
+
 struct ListOffsets {
   int off[TC_NUM_CLASSES];  // start of each class list inside the concatenated list buffer
 };
@@ -51,9 +54,11 @@ int launch_check(const int64_t *beg, const int32_t *adj, int64_t rows, int64_t m
 // One CSR: validation + class histogram + scatter in one kernel; class c (>= 1) is listed at
 // lists[(c-1) rows ...] and class_count[c] is its size.  lists holds 7 rows entries.
 // Rows outside [row_lo, row_hi) (row_hi < 0: all rows) are validated but classed as skipped.
+// alt_lists (7 rows entries, or null): every row also classed under the plain split there.
 int launch_check_classify(const int64_t *beg, const int32_t *adj, int64_t rows, int64_t m, int check_ids,
                           int min_deg, int warp_max, int cta_max, int schedule, TcControl *ctl, int *lists,
-                          int num_sms, cudaStream_t st, int64_t row_lo = 0, int64_t row_hi = -1);
+                          int num_sms, cudaStream_t st, int64_t row_lo = 0, int64_t row_hi = -1,
+                          int *alt_lists = nullptr);
 int launch_classify(int pass, const int64_t *begA, const int64_t *begB, int64_t rows, int min_deg,
                     int warp_max, int cta_max, TcControl *ctl, int *lists, const ListOffsets &off,
                     int num_sms, cudaStream_t st, int schedule = TRUST_TC_SCHED_TUNED,
