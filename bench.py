@@ -393,7 +393,11 @@ def run_ours(args, ws, rank, local):
     tuned_cfg, _ = T.autotune(beg, adj, ctx, repeats=1 if big else 3,
                               time_budget_s=24.0 if big else 0.0)  # outside every timed region
     autotune_s = time.perf_counter() - t_tune
+    # gate_only: the same tuned classes and direction split without the network (the split taken
+    # whenever the rows allow it, no promotions, no heaviest-first order)
     runs = (("autotuned", lambda: T.count_csr(beg, adj, ctx=ctx, stream=stream.cuda_stream, **tuned_cfg)),
+            ("gate_only", lambda: T.count_csr(beg, adj, ctx=ctx, stream=stream.cuda_stream, schedule=T.SCHED_TUNED,
+                                              direction_split=1)),
             ("tuned", lambda: call(T.SCHED_TUNED)), ("plain", lambda: call(T.SCHED_PLAIN)))
     for name, fn in runs:
         fn()
@@ -495,6 +499,7 @@ def run_ours(args, ws, rank, local):
                          + (", fits in L2)" if 8 * (n + 1) + 4 * m < 126e6 else ", larger than L2)")},
         "schedules": sched,
         "learned_vs_plain": sched["learned"]["gteps"] / sched["plain"]["gteps"],
+        "learned_vs_gate_only": sched["learned"]["gteps"] / sched["gate_only"]["gteps"],
         "counts_consistent": ok,
         "kernel_ms": kernel_s * 1e3,
         "count_kernel_ms": count_s * 1e3,
@@ -628,6 +633,18 @@ def run_batch(args, ws, rank, local):
     e2e_ms = p0.elapsed_time(p1) / k_pipe
     bt2.close()
     del beg2, adj2
+    # one persistent launch over the whole union (every graph's rows in one count call, tuned
+    # classes, no per-graph attribution): what a single launch for all size classes would cost
+    union_ms = []
+    for i in range(5):
+        flush.fill_(i)
+        a_, b_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a_.record(stream)
+        ru = T.count_csr(beg, adj, ctx=ctx, stream=stream.cuda_stream, schedule=T.SCHED_TUNED)
+        b_.record(stream)
+        torch.cuda.synchronize()
+        union_ms.append(a_.elapsed_time(b_))
+        ok = ok and ru.triangles == int(expect.sum())
     # the plain schedule, one call per graph (device-resident per-graph CSRs made beforehand)
     per = [B.graph_csr(beg, adj, gv, g) for g in range(gv.size - 1)]
     torch.cuda.synchronize()
@@ -670,6 +687,10 @@ def run_batch(args, ws, rank, local):
         "schedules": {"batched_autotuned": {"gteps": m / (statistics.median(step_ms) * 1e-3) / 1e9,
                                             "ms": statistics.median(step_ms)},
                       "batched_default": {"gteps": m / (default_ms * 1e-3) / 1e9, "ms": default_ms},
+                      "union_one_launch": {"gteps": m / (statistics.median(union_ms) * 1e-3) / 1e9,
+                                           "ms": statistics.median(union_ms),
+                                           "note": "the union CSR in one count call (tuned classes), total "
+                                                   "only: no per-graph counts"},
                       "plain_loop_per_graph": {"gteps": m / (min(loop_ms) * 1e-3) / 1e9, "ms": min(loop_ms)}},
         "learned_vs_plain": min(loop_ms) / statistics.median(step_ms),
         "counts_consistent": ok,

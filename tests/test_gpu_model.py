@@ -74,7 +74,7 @@ def test_learned_schedule_exact_with_any_model(seed):
         m[mlp.OFF_YMEAN], m[mlp.OFF_YSCALE] = log2_cycles, 1.0
         return m
 
-    models = [T.model_init(seed=seed), constant_model(25.0), constant_model(0.0)]
+    models = [T.model_init(seed=seed), constant_model(27.0), constant_model(0.0)]
     d = T.model_default()
     if d is not None:
         models.append(d)
@@ -85,7 +85,7 @@ def test_learned_schedule_exact_with_any_model(seed):
                 assert r.triangles == expect
         deg = np.diff(b)
         # (a graph this small only gets the scheduling pass when the split is forced)
-        # predicted 2^25 cycles: every warp-class row promoted to a CTA
+        # predicted 2^27 cycles (above the 2^26 promotion bound): every warp-class row promoted to a CTA
         r = T.count_csr(beg, adj, ctx=ctx, schedule=T.SCHED_LEARNED, model=models[1], direction_split=1)
         assert r.class_sizes["warp"] == 0 and r.class_sizes["cta"] == int(np.sum((deg > 32) & (deg <= 4096)))
         # predicted 1 cycle: the tuned classes stay
@@ -93,36 +93,42 @@ def test_learned_schedule_exact_with_any_model(seed):
         assert r.class_sizes["warp"] == int(np.sum((deg > 32) & (deg <= 512)))
 
 
-def test_learned_schedule_gain_on_skewed_rmat():
-    """What the trained network buys on a skewed graph (R-MAT scale 20, edge factor 16), against
-    (a) the plain degree-threshold schedule and (b) the same learned schedule with a network that
-    predicts nothing (all weights zero: every row at 1 cycle, so no predicted saving and no
-    direction split).  Same count every time; the trained network's predicted saving turns the
-    reverse-direction pass on and the call gets shorter (measured on GB300: 6.0 ms against 10.3 ms
-    plain; without the network the scheduling pass runs but nothing is split, as slow as the tuned
-    classes plus the pass; asserted with wide margins)."""
+def _median_call(beg, adj, ctx, reps=5, **kw):
     import statistics
-    pairs = T.gen_rmat(20, 16, seed=3)
-    beg, adj = T.build_csr(pairs, 1 << 20)
+    ts, r = [], None
+    for _ in range(reps):
+        r = T.count_csr(beg, adj, ctx=ctx, **kw)
+        ts.append(r.call_seconds)
+    return statistics.median(ts), r
+
+
+@pytest.mark.parametrize("scale,ef,a,seed", [(20, 16, 0.57, 3), (24, 16, 0.70, 3)])
+def test_learned_schedule_gain_on_skewed_rmat(scale, ef, a, seed):
+    """What the trained network buys on a skewed graph (R-MAT 20, and the held-out R-MAT 24 with
+    a = 0.70), against three arms: (a) the plain degree-threshold schedule; (b) the same learned
+    schedule with a network that predicts nothing (all weights zero: every row at 1 cycle, so no
+    predicted saving and no direction split); (c) the gate alone: the tuned classes with the
+    split taken whenever the rows allow it, no network.  Same count every time.  Measured on GB300
+    (call ms): R-MAT 20 learned 5.66, gate-only 5.91, plain 10.2; R-MAT 24 a = 0.70 learned 169.6
+    (promotions off), gate-only 169.4, plain 334.  The network turns the split on where the gate
+    would; against the gate alone it is equal within noise on the large graph (asserted: no worse
+    than 5 %), and faster on R-MAT 20."""
+    b_ = (1.0 - a - 0.05) / 2
+    pairs = T.gen_rmat(scale, ef, a, b_, b_, seed=seed)
+    beg, adj = T.build_csr(pairs, 1 << scale)
     del pairs
     blind = np.zeros(mlp.FLOATS, dtype=np.float32)
     blind[mlp.OFF_ISCALE:mlp.OFF_ISCALE + 8] = 1.0
     blind[mlp.OFF_YSCALE] = 1.0
-    times = {}
-    counts = {}
     with T.Context() as ctx:
-        for name, sched, model in (("plain", T.SCHED_PLAIN, None), ("learned", T.SCHED_LEARNED, None),
-                                   ("no_network", T.SCHED_LEARNED, blind)):
-            ts = []
-            for _ in range(5):
-                r = T.count_csr(beg, adj, ctx=ctx, schedule=sched, model=model)
-                ts.append(r.call_seconds)
-            times[name] = statistics.median(ts)
-            counts[name] = r.triangles
-            if name == "learned":
-                assert r.direction_split and r.split_saving_ms > 1.0
-            if name == "no_network":
-                assert not r.direction_split and r.split_saving_ms < 0.01
-    assert counts["learned"] == counts["plain"] == counts["no_network"]
-    assert times["learned"] < 0.85 * times["plain"], times
-    assert times["learned"] < 0.95 * times["no_network"], times
+        t_plain, r_plain = _median_call(beg, adj, ctx, schedule=T.SCHED_PLAIN)
+        t_learned, r_learned = _median_call(beg, adj, ctx)
+        t_blind, r_blind = _median_call(beg, adj, ctx, model=blind)
+        t_gate, r_gate = _median_call(beg, adj, ctx, schedule=T.SCHED_TUNED, direction_split=1)
+    assert r_learned.triangles == r_plain.triangles == r_blind.triangles == r_gate.triangles
+    assert r_learned.direction_split and r_learned.split_saving_ms > 1.0
+    assert not r_blind.direction_split and r_blind.split_saving_ms < 0.01
+    assert r_gate.direction_split
+    assert t_learned < 0.85 * t_plain, (t_learned, t_plain)
+    assert t_learned < 0.95 * t_blind, (t_learned, t_blind)
+    assert t_learned <= 1.05 * t_gate, (t_learned, t_gate)

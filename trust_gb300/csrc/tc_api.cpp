@@ -166,9 +166,11 @@ static int resolve_cfg(trust_tc_ctx *c, const trust_tc_opts &o, bool same, Launc
 }
 
 // The learned schedule promotes a warp-class row to a CTA when its predicted cost exceeds
-// 2^TC_PROMOTE_LOG2 cycles (about 2 ms at the GB300 clock: only rows that would hold one warp
-// far longer than the rest of the queue).
-constexpr float TC_PROMOTE_LOG2 = 22.f;
+// 2^TC_PROMOTE_LOG2 cycles (about 32 ms at the GB300 clock: only a row that would hold one warp
+// far longer than the whole count).  Measured on GB300 (learned call): with the bound at 2^22 the
+// promotions cost 1-2 % (R-MAT 24 a = 0.70 172.1 against 169.6 ms without, R-MAT 26 ef32 2353
+// against 2335 ms, R-MAT 20 5.66 against 5.69 ms), so only outliers are promoted.
+constexpr float TC_PROMOTE_LOG2 = 26.f;
 
 // Below this many arcs the learned schedule's scheduling pass cannot be repaid: on R-MAT scale 18
 // (3.8M arcs, a 1.7 ms count) the split with the pass costs 2 % more than the tuned classes
