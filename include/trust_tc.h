@@ -280,16 +280,18 @@ int trust_tc_autotune(trust_tc_ctx *ctx, const int64_t *begin, const int32_t *ad
  * A batch is the disjoint union of many oriented graphs in one device CSR (ids global), graph g
  * owning rows [graph_vbeg[g], graph_vbeg[g+1]) and no arc leaving its graph (build it with
  * trust_tc_build_batch_device).  Graphs fall into TRUST_TC_BATCH_CLASSES size classes by vertex
- * count ([0,512), [512,4096), [4096,32768), [32768,...)), each counted by its own persistent
- * kernel with its own launch parameters; validation, classification, list offsets, the kernels
- * and the readback of the per-graph counts are captured in one CUDA graph at creation and
- * replayed by every run.  No counterpart in the reference, which counts one graph per run
- * (Without-graph-partition/mpi_main.cpp:75-119); the per-graph counts equal its counts. */
+ * count ([0,512), [512,4096), [4096,32768), [32768,...)), each with its own warp-class bound;
+ * every row of every graph is then counted by one persistent kernel launch.  Validation,
+ * classification, list offsets, that launch and the readback of the per-graph counts are captured
+ * in one CUDA graph at creation and replayed by every run.  No counterpart in the reference, which
+ * counts one graph per run (Without-graph-partition/mpi_main.cpp:75-119); the per-graph counts
+ * equal its counts. */
 #define TRUST_TC_BATCH_CLASSES 4
 typedef struct trust_tc_batch_class {
-  int threads_per_block; /* 64..1024, multiple of 32 (default 256)                            */
+  int threads_per_block; /* 64..1024, multiple of 32 (default 256); the one launch uses the value
+                            of the largest size class present                                 */
   int warp_max_degree;   /* out-degree above which a vertex gets a whole CTA (default 128)     */
-  int chunk;             /* vertices per queue claim (default 8)                               */
+  int chunk;             /* vertices per queue claim (default 8); as threads_per_block        */
 } trust_tc_batch_class;
 typedef struct trust_tc_batch trust_tc_batch;
 
@@ -304,9 +306,10 @@ int trust_tc_batch_info(const trust_tc_batch *batch, int64_t *graphs, int64_t *v
 int trust_tc_batch_get_class(const trust_tc_batch *batch, int size_class, trust_tc_batch_class *cfg);
 /* sets one size class's launch parameters and re-captures the job */
 int trust_tc_batch_set_class(trust_tc_batch *batch, int size_class, const trust_tc_batch_class *cfg);
-/* Times every size class's kernel under each candidate (threads 128/256/512/1024 x warp bound
- * 64/128 x chunk 2/4/8/16, `repeats` runs each, fastest kept), keeps the fastest configuration
- * per class and re-captures the job; *best_ms = the sum of the chosen kernels' times. */
+/* Times the counting launch under each candidate (threads 128/256/512/1024 x warp bound 64/128 x
+ * chunk 2/4/8/16, the same for every size class, `repeats` runs each, fastest kept), then each
+ * size class's warp bound on its own, keeps the fastest and re-captures the job; *best_ms = the
+ * chosen launch's time. */
 int trust_tc_batch_autotune(trust_tc_batch *batch, int repeats, double *best_ms);
 /* One launch of the captured job on `stream` (waits for it).  counts: host array of num_graphs
  * uint64 per-graph triangle counts (or NULL); result: totals, call_seconds = the graph's

@@ -605,15 +605,24 @@ __global__ void batch_class_kernel(const int64_t *__restrict__ beg, int64_t rows
   }
 }
 
-// List offsets of every (size class, degree class), in that order, from the histogram.
+// List offsets of every (size class, degree class), degree class major: each degree class's rows
+// of all size classes are contiguous, so ctl[nsc] (the combined block) describes them as one list
+// per degree class, drained by one persistent counting kernel.
 __global__ void batch_offsets_kernel(TcControl *ctl, int nsc) {
   if (blockIdx.x != 0 || threadIdx.x != 0) return;
   int run = 0;
-  for (int s = 0; s < nsc; ++s)
-    for (int c = 0; c < TC_NUM_CLASSES; ++c) {
+  for (int c = 0; c < TC_NUM_CLASSES; ++c) {
+    ctl[nsc].class_off[c] = run;
+    int all = 0;
+    for (int s = 0; s < nsc; ++s) {
       ctl[s].class_off[c] = run;
-      if (c > TC_CLASS_SKIP) run += ctl[s].class_count[c];
+      if (c > TC_CLASS_SKIP) {
+        run += ctl[s].class_count[c];
+        all += ctl[s].class_count[c];
+      }
     }
+    ctl[nsc].class_count[c] = all;
+  }
 }
 
 int launch_batch_classify(int pass, const int64_t *beg, int64_t rows, const int *graph_of,
