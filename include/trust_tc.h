@@ -106,7 +106,9 @@ typedef struct trust_tc_result {
   uint64_t triangles;       /* the count                                                     */
   double kernel_seconds;    /* CUDA-event time of classification + counting (validation too in
                                a single-graph call, where it runs fused with classification) */
-  double count_seconds;     /* CUDA-event time of the counting kernel alone                  */
+  double count_seconds;     /* CUDA-event time of the counting kernels alone (with the direction
+                               split: from the first counting launch to the end of whichever of
+                               the two concurrent passes ends last)                          */
   double call_seconds;      /* CUDA-event time of the whole device-side call                 */
   int64_t vertices;         /* n                                                            */
   int64_t edges;            /* m (oriented arcs = undirected edges)                         */

@@ -503,15 +503,19 @@ int count_device(trust_tc_ctx *c, const DevGraph3 &g, const trust_tc_opts &o, bo
   TC_CUDA_TRY(cudaEventElapsedTime(&t_kernel, c->ev[1], c->ev[3]));
   TC_CUDA_TRY(cudaEventElapsedTime(&t_count, c->ev[2], c->ev[3]));
   TC_CUDA_TRY(cudaEventElapsedTime(&t_call, c->ev[0], c->ev[4]));
-  if (split) {  // classification to the end of whichever pass ends last
-    float t_end_b = 0;
+  if (split) {  // classification (counting) to the end of whichever pass ends last
+    float t_end_b = 0, t_count_b = 0;
     TC_CUDA_TRY(cudaEventElapsedTime(&t_end_b, c->ev[1], c->ev_split[2]));
+    TC_CUDA_TRY(cudaEventElapsedTime(&t_count_b, c->ev[2], c->ev_split[2]));
     t_kernel = std::max(t_kernel, t_end_b);
+    t_count = std::max(t_count, t_count_b);
   }
   r->triangles = done.count + rb.triangles;
   r->wedges = (int64_t)done.wedges + rb.wedges;
   r->kernel_seconds = t_kernel * 1e-3;
-  r->count_seconds = t_count * 1e-3 + rb.count_seconds;  // both passes' count kernels
+  // the counting kernels' wall span: from the first pass's first counting launch to the end of
+  // whichever pass ends last (the two passes run at the same time on two streams)
+  r->count_seconds = t_count * 1e-3;
   r->call_seconds = t_call * 1e-3;
   r->max_out_degree = done.max_out_degree;
   for (int k = 0; k < TC_NUM_CLASSES; ++k) r->class_sizes[k] = h.class_count[k];

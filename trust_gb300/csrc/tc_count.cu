@@ -1177,10 +1177,13 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned pari
   }
 }
 
-// Persistent over the huge list: cluster k takes hubs k, k + clusters, ...; rows longer than
-// p.hub_max_degree are left to the main kernel's spill tables.  Every cluster.sync() is reached
-// by all CTAs of the cluster (the loop bounds and the skip test are the same for all of them);
-// no remote access happens before the first sync of a hub, and none after the final sync.
+// Persistent over the huge list: a cluster claims hubs one at a time from a counter (rank 0 claims,
+// the cluster reads the claim from its shared memory), so the heaviest-first order of the list
+// becomes a longest-first schedule instead of a fixed round-robin whose heaviest clusters set the
+// tail; rows longer than p.hub_max_degree are left to the main kernel's spill tables.  Every
+// cluster.sync() is reached by all CTAs of the cluster (the claim, the loop exit and the skip
+// test are the same for all of them); no remote access happens before the first sync of a hub,
+// and none after the final sync.
 // Each CTA stages its contiguous share of the hub row with one TMA bulk copy (the 16-byte aligned
 // interior; the ragged ends, at most 3 entries each, by plain loads) and inserts from shared
 // memory.  Dynamic shared memory: the table share (2^share_log2_max ints) then the staging buffer.
@@ -1197,6 +1200,7 @@ __global__ void __launch_bounds__(512, 2) hub_kernel(CountArgs p, int log2C, int
   __shared__ int tma_ok;
   __shared__ int abandoned;  // 1 + parity of a barrier phase whose copy this CTA stopped waiting for
   __shared__ int n_ov;       // quotient table: keys in the overflow list
+  __shared__ int claimed;    // rank 0: the hub this cluster claimed
   // dynamic shared memory: the table share, the quotient table's overflow list, the staging buffer
   int *ov = smem + (1 << share_log2_max);
   int *stage = ov + TC_Q16_OVERFLOW;
@@ -1211,13 +1215,18 @@ __global__ void __launch_bounds__(512, 2) hub_kernel(CountArgs p, int log2C, int
   const int C = 1 << log2C;
   const int rank = (int)cl.block_rank();
   const int lane = threadIdx.x & 31;
-  const int clusters = gridDim.x >> log2C;
-  const int cid = blockIdx.x >> log2C;
   const int n_items = p.ctl->class_count[TC_CLASS_HUGE];
   const int *list = class_list(p, TC_CLASS_HUGE);
   int *ctr = cl.map_shared_rank(&next_batch, 0);
   unsigned long long hits = 0, wedges = 0;
-  for (int t = cid; t < n_items; t += clusters) {
+  // hub claims: class_next[TC_CLASS_SKIP], a head no counting queue uses
+  int *claim_src = cl.map_shared_rank(&claimed, 0);
+  for (;;) {
+    if (rank == 0 && threadIdx.x == 0) claimed = atomicAdd(&p.ctl->class_next[TC_CLASS_SKIP], 1);
+    cl.sync();
+    const int t = *claim_src;
+    cl.sync();  // every CTA has read the claim before rank 0 makes the next one
+    if (t >= n_items) break;
     const int v = list[t];
     int bA, dA, bB, dB;
     row_of(p.begA, arow(p, v), bA, dA);
