@@ -67,15 +67,16 @@ def _peaks():
 
 
 def _traffic(workload):
-    """DRAM bytes per counting-kernel launch from the committed ncu summary, if one exists."""
+    """(DRAM bytes of the counting kernels of one call, how they were obtained) from the committed
+    ncu summaries (profiles/traffic.json), or (None, reason)."""
     p = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(p):
         with open(p) as f:
             d = json.load(f)
         e = d.get(workload)
         if e:
-            return e.get("dram_bytes_per_launch")
-    return None
+            return e.get("dram_bytes_per_call"), e.get("source")
+    return None, "no ncu capture of this workload"
 
 
 class ClockSampler:
@@ -512,9 +513,11 @@ def run_ours(args, ws, rank, local):
                         "to after the last result read",
                 "serial": {"value": m / (e2e_serial_mean * 1e-3) / 1e9, "ms_per_step": e2e_serial_mean}},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": _traffic(args.workload), "peak_source": peak_src,
+                     "traffic": _traffic(args.workload)[0], "traffic_source": _traffic(args.workload)[1],
+                     "peak_source": peak_src,
                      "algorithmic_bytes": algo_bytes,
-                     "bytes_formula": "24 m + 8 (n+1) + 4 W (W = wedges = probes)"},
+                     "bytes_formula": "24 m + 8 (n+1) + 4 W (W = wedges = probes made, both passes of the "
+                                      "direction split); time = the counting kernels' wall span (count_kernel_ms)"},
         "preprocess": {"gpu_generate_ms": prep["generate_ms"], "gpu_build_csr_ms": prep["preprocess_ms"]},
         "clocks": clocks,
     }
