@@ -394,11 +394,14 @@ def run_ours(args, ws, rank, local):
     tuned_cfg, _ = T.autotune(beg, adj, ctx, repeats=1 if big else 3,
                               time_budget_s=24.0 if big else 0.0)  # outside every timed region
     autotune_s = time.perf_counter() - t_tune
-    # gate_only: the same tuned classes and direction split without the network (the split taken
-    # whenever the rows allow it, no promotions, no heaviest-first order)
+    # gate_only: the tuned classes with the direction split decided by the learned schedule's gate
+    # alone (at least 2^22 arcs, a row of at least 64 entries, at least 15 % of the arcs in rows
+    # longer than 128), no network: no promotions, no heaviest-first order
+    deg = beg[1:] - beg[:-1]
+    gate = bool(m >= (1 << 22) and int(deg.max()) >= 64 and int(deg[deg > 128].sum()) >= 0.15 * m)
     runs = (("autotuned", lambda: T.count_csr(beg, adj, ctx=ctx, stream=stream.cuda_stream, **tuned_cfg)),
             ("gate_only", lambda: T.count_csr(beg, adj, ctx=ctx, stream=stream.cuda_stream, schedule=T.SCHED_TUNED,
-                                              direction_split=1)),
+                                              direction_split=1 if gate else 0)),
             ("tuned", lambda: call(T.SCHED_TUNED)), ("plain", lambda: call(T.SCHED_PLAIN)))
     for name, fn in runs:
         fn()
@@ -417,6 +420,8 @@ def run_ours(args, ws, rank, local):
         if name == "autotuned":
             sched[name]["launch"] = tuned_cfg
             sched[name]["autotune_s"] = autotune_s
+        if name == "gate_only":
+            sched[name]["gate_passes"] = gate
 
     # the n x n tile loop on the same graph (once per mode, outside the timed region): tiles in HBM
     # under the learned and the plain schedule, and streamed through a 3.5-tile device budget
