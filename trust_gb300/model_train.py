@@ -8,7 +8,15 @@ For every vertex with out-degree >= 2 the counting kernel records its clock64 cy
 (tuned schedule, no direction split) and trust_tc_vertex_features gives its 8 features; the
 target is log2(cycles).  The MLP is trained by the library's own CUDA forward/backward/Adam
 kernels.  Held out: R-MAT scale 24 with a = 0.70 and the 4096 x 4096 triangulated grid (one
-diagonal per cell).  The report gives the predictor's error per graph.
+diagonal per cell).  The report gives the predictor's error per graph and, for the held-out graphs,
+the time and TEPS of one counting call under the learned schedule (with the trained model), the
+gate alone (tuned classes, direction split exactly when the learned schedule's gate passes), the
+tuned classes and TRUST's plain split.
+
+    python -m trust_gb300.model_train --held-out-only --report FILE
+
+times the held-out graphs with the model compiled into the library and replaces the report's
+held-out entries, without training.
 """
 from __future__ import annotations
 
@@ -70,6 +78,70 @@ def samples(beg, adj, ctx):
     return x, y, r
 
 
+def gate_passes(beg) -> bool:
+    """The learned schedule's gate: >= 2^22 arcs, a row of >= 64 entries, >= 15 % of the arcs in
+    rows longer than 128 entries."""
+    deg = (beg[1:] - beg[:-1])
+    m = int(deg.sum())
+    return bool(m >= (1 << 22) and int(deg.max()) >= 64 and int(deg[deg > 128].sum()) >= 0.15 * m)
+
+
+def time_schedules(beg, adj, ctx, model, warmup=3, reps=5):
+    """Median CUDA-event time of one counting call per schedule (256 MiB written before each
+    call so the graph is not served from L2), every schedule's count checked equal."""
+    import torch
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    gate = gate_passes(beg)
+    arms = {
+        "learned": lambda: T.count_csr(beg, adj, ctx=ctx, model=model),
+        "gate_only": lambda: T.count_csr(beg, adj, ctx=ctx, schedule=T.SCHED_TUNED,
+                                         direction_split=1 if gate else 0),
+        "tuned": lambda: T.count_csr(beg, adj, ctx=ctx, schedule=T.SCHED_TUNED, direction_split=0),
+        "plain": lambda: T.count_csr(beg, adj, ctx=ctx, schedule=T.SCHED_PLAIN),
+    }
+    out, counts = {"gate_passes": gate}, set()
+    edges = adj.numel()
+    for name, fn in arms.items():
+        for _ in range(warmup):
+            counts.add(fn().triangles)
+        ts = []
+        for _ in range(reps):
+            flush.fill_(1)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            r = fn()
+            e1.record()
+            torch.cuda.synchronize()
+            counts.add(r.triangles)
+            ts.append(e0.elapsed_time(e1))
+        ms = float(np.median(ts))
+        out[name] = {"ms": ms, "gteps": edges / (ms * 1e-3) / 1e9}
+    if len(counts) != 1:
+        raise RuntimeError(f"schedules disagree on the count: {sorted(counts)}")
+    out["triangles"] = counts.pop()
+    out["learned_vs_plain"] = out["plain"]["ms"] / out["learned"]["ms"]
+    out["learned_vs_gate_only"] = out["gate_only"]["ms"] / out["learned"]["ms"]
+    return out
+
+
+def held_out_entry(kind, p1, p2, ctx, model):
+    import torch
+    beg, adj = make_graph(kind, p1, p2, seed=900)
+    x, y, r = samples(beg, adj, ctx)
+    p = T.model_predict(x, model)
+    err = (p - y).abs()
+    long_rows = x[:, 0] > np.log2(33.0)
+    entry = {"graph": f"{kind}-{p1}-{p2}", "vertices": r.vertices, "edges": r.edges, "rows": int(x.shape[0]),
+             "mae_log2": float(err.mean()), "median_abs_log2": float(err.median()),
+             "rows_over_32": int(long_rows.sum())}
+    if int(long_rows.sum()) > 0:
+        entry["mae_log2_rows_over_32"] = float(err[long_rows].mean())
+    entry["schedules"] = time_schedules(beg, adj, ctx, model)
+    entry["gpu"] = torch.cuda.get_device_name()
+    del beg, adj
+    return entry
+
+
 def main():
     import torch
     ap = argparse.ArgumentParser()
@@ -77,9 +149,26 @@ def main():
     ap.add_argument("--report", default=None)
     ap.add_argument("--epochs", type=int, default=60)
     ap.add_argument("--per-graph", type=int, default=150_000, help="samples kept per training graph")
+    ap.add_argument("--held-out-only", action="store_true",
+                    help="time and score the held-out graphs with the compiled-in model; no training")
     args = ap.parse_args()
     torch.manual_seed(0)
     ctx = T.Context()
+    if args.held_out_only:
+        model = T.model_default()
+        if model is None:
+            raise SystemExit("no model compiled into the library")
+        report = {}
+        if args.report and os.path.exists(args.report):
+            with open(args.report) as fh:
+                report = json.load(fh)
+        report["held_out"] = [held_out_entry(kind, p1, p2, ctx, model) for kind, p1, p2 in HELD_OUT]
+        text = json.dumps(report, indent=1)
+        if args.report:
+            with open(args.report, "w") as fh:
+                fh.write(text + "\n")
+        print(text)
+        return
     xs, ys, report = [], [], {"train": [], "held_out": []}
     t0 = time.time()
     for i, (kind, p1, p2) in enumerate(TRAIN):
@@ -108,18 +197,7 @@ def main():
     pred = T.model_predict(X, model)
     report["train_rmse_log2"] = float(torch.sqrt(torch.mean((pred - Y) ** 2)))
     for kind, p1, p2 in HELD_OUT:
-        beg, adj = make_graph(kind, p1, p2, seed=900)
-        x, y, r = samples(beg, adj, ctx)
-        p = T.model_predict(x, model)
-        err = (p - y).abs()
-        long_rows = x[:, 0] > np.log2(33.0)
-        entry = {"graph": f"{kind}-{p1}-{p2}", "vertices": r.vertices, "edges": r.edges, "rows": int(x.shape[0]),
-                 "mae_log2": float(err.mean()), "median_abs_log2": float(err.median()),
-                 "rows_over_32": int(long_rows.sum())}
-        if int(long_rows.sum()) > 0:
-            entry["mae_log2_rows_over_32"] = float(err[long_rows].mean())
-        report["held_out"].append(entry)
-        del beg, adj
+        report["held_out"].append(held_out_entry(kind, p1, p2, ctx, model))
     report["seconds"] = time.time() - t0
     with open(args.out, "w") as fh:
         fh.write("/* cost model trained by trust_gb300/model_train.py on the GPU; %d floats */\n" % model.size)
