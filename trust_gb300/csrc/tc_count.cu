@@ -257,13 +257,50 @@ __device__ __forceinline__ int group_has(const int *wtab, int g, int w) {
   }
 }
 
-// Probe every wedge of a warp whose lanes hold one arc each, lanes [gG, gG+G) belonging to
-// vertex g.  Unlike probe_arcs, the wedges of all groups are flattened into one list over the
-// 32 lanes, so a round costs the same whatever the spread of work between groups; a wedge finds
-// its arc by a shuffle binary search and its group's set by the arc's lane.  Rows of at least
-// 32 * TC_UNROLL entries are walked by the whole warp instead (keeps wedge indices small).
+// Membership of w in a row of at most G keys held in registers (-1 past the row; w >= 0).
 template <int G>
-__device__ __forceinline__ void probe_warp_flat(const int32_t *__restrict__ adjC, int s, int dd,
+__device__ __forceinline__ unsigned match_keys(int w, const int (&key)[G]) {
+  bool m = false;
+#pragma unroll
+  for (int k = 0; k < G; ++k) m |= w == key[k];
+  return m;
+}
+
+// One lane walks its own arc's target row against its vertex's keys in registers: the first eight
+// entries and the next four are loaded before any is matched (most of these rows are that short),
+// then four at a time with the next four in flight.  -2 marks entries past the row.
+template <int G>
+__device__ __forceinline__ unsigned lane_walk(const int32_t *__restrict__ row, int d, const int (&key)[G]) {
+  unsigned h = 0;
+  int w[8];
+#pragma unroll
+  for (int r = 0; r < 8; ++r) w[r] = r < d ? tc_ld_nc(row + r) : -2;
+  int n0 = -2, n1 = -2, n2 = -2, n3 = -2;
+  if (d > 8) {
+    n0 = tc_ld_nc(row + 8);
+    n1 = 9 < d ? tc_ld_nc(row + 9) : -2;
+    n2 = 10 < d ? tc_ld_nc(row + 10) : -2;
+    n3 = 11 < d ? tc_ld_nc(row + 11) : -2;
+  }
+#pragma unroll
+  for (int r = 0; r < 8; ++r) h += match_keys<G>(w[r], key);
+  for (int k = 8; k < d; k += 4) {
+    const int m0 = k + 4 < d ? tc_ld_nc(row + k + 4) : -2, m1 = k + 5 < d ? tc_ld_nc(row + k + 5) : -2,
+              m2 = k + 6 < d ? tc_ld_nc(row + k + 6) : -2, m3 = k + 7 < d ? tc_ld_nc(row + k + 7) : -2;
+    h += match_keys<G>(n0, key) + match_keys<G>(n1, key) + match_keys<G>(n2, key) + match_keys<G>(n3, key);
+    n0 = m0; n1 = m1; n2 = m2; n3 = m3;
+  }
+  return h;
+}
+
+// Probe every wedge of a warp whose lanes hold one arc each, lanes [gG, gG+G) belonging to
+// vertex g.  Rows of at least 32 * TC_UNROLL entries are walked by the whole warp.  Shorter rows:
+// for G <= 8 each lane walks its own row; for G >= 16 the wedges of all groups are flattened into
+// one list over the 32 lanes, so a round costs the same whatever the spread of work between
+// groups, and a wedge finds its arc by a shuffle binary search and its group's set by the arc's
+// lane.
+template <int G>
+__device__ __forceinline__ void probe_warp_flat(const int32_t *__restrict__ adjC, int s, int dd, int uA,
                                                 const int *wtab, unsigned long long &hits,
                                                 unsigned long long &wedges) {
   constexpr int U = TC_UNROLL;
@@ -298,6 +335,18 @@ __device__ __forceinline__ void probe_warp_flat(const int32_t *__restrict__ adjC
   // arcs starting inside the round: owner rank = arcs started before the round + starts at or
   // before this lane's position - 1.
   const int sd = dd < LONG ? dd : 0;
+  if constexpr (G <= 8) {
+    // Rows of at most 8 keys: each lane walks its own arc's target row against its vertex's keys
+    // held in registers.  A step then costs its longest short row in steps of a few instructions,
+    // where flattening costs an owner search per 32 wedges and the ranking of the arcs (Chung-Lu
+    // 3.8 M: count 0.408 -> 0.348 ms; 4096x4096 grid: 0.730 -> 0.446 ms; R-MAT 22: 25.1 -> 24.9 ms;
+    // keys of 16 in registers were slower on every graph measured).
+    int key[G];
+#pragma unroll
+    for (int k = 0; k < G; ++k) key[k] = __shfl_sync(TC_FULL_MASK, uA, (lane & ~(G - 1)) + k);
+    hits += lane_walk<G>(adjC + s, sd, key);
+    return;
+  }
   const int incl = group_scan_incl<32>(sd, lane);
   const int tot = __shfl_sync(TC_FULL_MASK, incl, 31);
   if (tot == 0) return;
@@ -659,8 +708,9 @@ struct BlockShared {
 };
 
 // Neighbour rows at least this long are set aside by the 32-arc batch pass of a CTA vertex and
-// then claimed one row per warp, so one batch full of long rows no longer holds up the CTA.
-constexpr int TC_CTA_LONG = 256;
+// then claimed one row per warp, so one batch full of long rows no longer holds up the CTA
+// (128 against 256: R-MAT 22 24.98 -> 24.61 ms, R-MAT 26 2270 -> 2262 ms of counting).
+constexpr int TC_CTA_LONG = 128;
 
 // Walk one neighbour row with a whole warp: 32 * 2 TC_UNROLL entries per step, next step's loads
 // issued before the current step is probed (R-MAT 26: 4 % faster than 4 loads per lane, the bytes
@@ -900,7 +950,7 @@ __device__ __forceinline__ void group_vertex(const CountArgs &p, int uA, int s, 
     if (uA >= 0) set_insert(tab, LOG2, uA);
   }
   __syncwarp();
-  probe_warp_flat<G>(p.adjC, s, dd, wtab, hits, wedges);
+  probe_warp_flat<G>(p.adjC, s, dd, uA, wtab, hits, wedges);
   __syncwarp();
 }
 
