@@ -41,13 +41,13 @@ WORKLOADS = {
                    desc="R-MAT scale 20 edge factor 16 (0.57,0.19,0.19,0.05) seed=3"),
     "rmat22": dict(kind="rmat", scale=22, ef=16, a=0.57, b=0.19, c=0.19, seed=3,
                    desc="R-MAT scale 22 edge factor 16 (0.57,0.19,0.19,0.05) seed=3"),
-    "rmat24_a070": dict(kind="rmat", scale=24, ef=16, a=0.70, b=0.125, c=0.125, seed=3,
+    "rmat24_a070": dict(kind="rmat", scale=24, ef=16, a=0.70, b=0.125, c=0.125, seed=3, default_steps=20,
                         desc="R-MAT scale 24 edge factor 16 (0.70,0.125,0.125,0.05) seed=3 (cost model held out)"),
-    "rmat26_ef32": dict(kind="rmat", scale=26, ef=32, a=0.57, b=0.19, c=0.19, seed=3, tiles=2,
+    "rmat26_ef32": dict(kind="rmat", scale=26, ef=32, a=0.57, b=0.19, c=0.19, seed=3, tiles=2, default_steps=20,
                         desc="R-MAT scale 26 edge factor 32 (0.57,0.19,0.19,0.05) seed=3"),
     "grid4096": dict(kind="grid", k=4096,
                      desc="4096 x 4096 grid with one diagonal per cell (triangulated mesh; cost model held out)"),
-    "batch4096": dict(kind="batch", graphs=4096, nmin=50, nmax=50_000, seed=5,
+    "batch4096": dict(kind="batch", graphs=4096, nmin=50, nmax=50_000, seed=5, default_steps=50,
                       desc="4096 graphs, vertices log-uniform 50..50,000, alternately Erdos-Renyi (avg degree "
                            "4..64) and Barabasi-Albert (2..16 edges per vertex), seed=5"),
 }
@@ -789,7 +789,9 @@ def run_reference(args, ws, rank, local):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default: 20 for R-MAT 24/26, whose calls take 0.17-2.3 s; 50 for the "
+                         "batch; 200 otherwise)")
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default=DEFAULT_WORKLOAD)
@@ -797,6 +799,8 @@ def main():
     ap.add_argument("--tiles", type=int, default=None,
                     help="also run the parts x parts tile loop (default: 2 for rmat26_ef32, else off)")
     args = ap.parse_args()
+    if args.steps is None:
+        args.steps = WORKLOADS[args.workload].get("default_steps", 200)
     if args.warmup < 3:
         args.warmup = 3
     ws, rank, local = _dist()
