@@ -12,10 +12,17 @@
 #                                           sm_103a; loaded on the GPU host by ref_tc_driver.c
 #                                           (the x86 host binaries here do not run there)
 #
-# Usage: oracle/build_ref.sh <reference_root>
+# Usage: oracle/build_ref.sh [<reference_root>]
+# Without an argument the reference is looked for at /root/reference, where the build container
+# mounts it; where it is absent (the GPU host, which uses the files built here) nothing is built.
 set -eu
-[ $# -eq 1 ] || { echo "usage: $0 <reference_root>" >&2; exit 2; }
-REF=$1
+[ $# -le 1 ] || { echo "usage: $0 [<reference_root>]" >&2; exit 2; }
+if [ $# -eq 1 ]; then
+  REF=$1
+else
+  REF=/root/reference
+  [ -d "$REF/Preprocess" ] || exit 0
+fi
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/_ref"
 mkdir -p "$OUT"

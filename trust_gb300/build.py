@@ -6,7 +6,7 @@ Outputs (all git-ignored):
   trust_gb300/trust_tc         the CLI with the reference's argv and output line
   oracle/_build/liboracle.so   CPU oracle (tests, smoke and the bench CPU legs only)
   oracle/_build/liboracle_cuda.so  oracle + the harness that runs the reference kernel cubin
-  oracle/_ref/*                the reference's own code, only where TRUST_REFERENCE_ROOT names its sources
+  oracle/_ref/*                the reference's own code, where its sources are present (oracle/build_ref.sh)
 
 Compiles in parallel and skips outputs newer than their sources.
 """
@@ -118,12 +118,13 @@ def build_oracle() -> None:
         _run(["gcc", "-O2", "-std=c11", "-ffp-contract=off", "-fPIC", "-shared", "-I" + os.path.join(cuda, "include"),
               "-o", ORACLE_CUDA_LIB, drv, src, "-L" + os.path.join(cuda, "lib64", "stubs"), "-lcuda",
               "-lpthread", "-lm"])
-    # the reference's own sources, where the caller names them (TRUST_REFERENCE_ROOT); without it
-    # the reference oracles are used only if an earlier build left them in oracle/_ref/
+    # the reference's own sources: where TRUST_REFERENCE_ROOT names them, else where the recipe
+    # finds them by default (it builds nothing where they are absent); a machine without them uses
+    # what an earlier build left in oracle/_ref/
     ref_root = os.environ.get("TRUST_REFERENCE_ROOT")
     ref_out = os.path.join(ORACLE, "_ref", "tc_ref_w.cubin")
-    if ref_root and os.path.isdir(os.path.join(ref_root, "Preprocess")) and not os.path.exists(ref_out):
-        _run(["sh", os.path.join(ORACLE, "build_ref.sh"), ref_root])
+    if not os.path.exists(ref_out) and (not ref_root or os.path.isdir(os.path.join(ref_root, "Preprocess"))):
+        _run(["sh", os.path.join(ORACLE, "build_ref.sh")] + ([ref_root] if ref_root else []))
 
 
 def build_all() -> None:
