@@ -85,6 +85,22 @@ def test_count_without_a_device_fails_loudly():
     assert e.value.status == _lib.E_NO_DEVICE
 
 
+def test_argument_errors_come_before_any_device_call():
+    """Bad source-row slices and schedules are refused before the library touches a device, so the
+    answer is E_ARG on any machine (the call never reaches the GPU)."""
+    beg = np.array([0, 2, 3, 3], dtype=np.int64)
+    adj = np.array([1, 2, 2], dtype=np.int32)
+    for rr in ((2, 1), (-1, 2), (0, 4), (4, 3)):
+        with pytest.raises(T.TrustTcError) as e:
+            T.count_csr(beg, adj, row_range=rr)
+        assert e.value.status == _lib.E_ARG, rr
+    with pytest.raises(ValueError):
+        T.count_csr(beg, adj, row_range=(0, 0))  # an explicit slice ends at a positive row
+    with pytest.raises(T.TrustTcError) as e:
+        T.count_csr(beg, adj, schedule=7)
+    assert e.value.status == _lib.E_ARG
+
+
 def test_folder_roundtrip_and_errors(tmp_path):
     z = np.load(os.path.join(ROOT, "tests", "golden", "rmat_s9.npz"))
     T.save_folder(str(tmp_path), z["ref_beg"], z["ref_adj"])
